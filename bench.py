@@ -1,0 +1,363 @@
+#!/usr/bin/env python
+"""NTT benchmark on GB300 -- the headline line is a single Goldilocks NTT.
+
+Default workload: one step = forward + inverse Goldilocks NTT of n = 2^24
+elements (128 MiB), in place, inputs resident in HBM, L2 flushed between
+steps (a 256 MiB write outside the timed events). Metric: Gelem/s =
+2 * n / step time (both transforms count).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME]
+    python bench.py --impl reference ...   # the reference's CPU path
+
+Multi-GPU: replicas only (the transform does not shard); every rank runs the
+same workload, value = all ranks' elements / max-over-ranks time.
+
+JSON keys beyond the base contract:
+  e2e           same metric through the C-ABI host-buffer call
+                (stntt_ntt_gl64_host: H2D, transform, D2H per call)
+  roofline      dominant kernel (the tile kernel): algorithmic bytes per
+                launch / mean launch time, against MEASURED_PEAKS.json hbm_gbs
+  cpu_baseline  the CPU oracle port of the reference loop on a bounded sample
+  clocks        nvidia-smi samples taken during the timed region
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOADS = {
+    # name: (field, log_n)
+    "gl64_2^24_fwd+inv": ("gl64", 24),
+    "gl64_2^20_fwd+inv": ("gl64", 20),
+    "u32_2^26_fwd+inv": ("u32", 26),
+    "u32_2^16_fwd+inv": ("u32", 16),
+}
+DEFAULT_WORKLOAD = "gl64_2^24_fwd+inv"
+METRIC = "NTT Gelem/s (Goldilocks 2^24 forward+inverse, per element transformed)"
+L2_BYTES = 129 * 1024 * 1024
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def peaks():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        try:
+            d = json.loads(f.read_text())
+            return float(d["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples (200 ms) while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits", "-lms", "100",
+                 "-i", str(self.gpu)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------- reference arm
+def run_reference(args):
+    """The reference's CPU NTT loop on all host threads (each thread one
+    independent transform). Goldilocks has no CPU code in the reference, so
+    this is the oracle's restatement of its Stockham loop (ntt_cpu.cpp:46-85)
+    with Goldilocks arithmetic ("port"); the 32-bit workloads use the
+    unmodified reference build when oracle/_ref loads here, else the port."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import oracle as O
+
+    field, lg = WORKLOADS[args.workload]
+    n = 1 << lg
+    threads = max(1, min(O.cpu_count(), 16))
+    kind = "port"
+    if field == "gl64":
+        x = O.uniform_u64(7, n * threads)
+
+        def step():
+            y = O.ntt_gl64(x, batch=threads, threads=threads)
+            O.ntt_gl64(y, inverse=True, batch=threads, threads=threads)
+    else:
+        root, p = O.find_params(n, 11)
+        x = O.uniform_u32(7, p, n * threads)
+
+        def step():
+            y = O.ntt_u32(x, root, p, batch=threads, threads=threads)
+            O.ntt_u32(y, root, p, inverse=True, batch=threads, threads=threads)
+    steps = max(1, min(args.steps, 3))
+    warm = min(args.warmup, 1)
+    for _ in range(warm):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    dt = (time.perf_counter() - t0) / steps
+    val = 2 * n * threads / dt / 1e9
+    sample = (f"{threads} independent {field} 2^{lg} forward+inverse transforms per step, one per host thread; "
+              f"{steps} timed steps after {warm} warm-up (steps capped so the CPU run stays within minutes)")
+    line = {
+        "impl": "reference", "metric": METRIC if args.workload == DEFAULT_WORKLOAD else f"NTT Gelem/s ({args.workload})",
+        "value": val, "unit": "Gelem/s", "n_gpus": world, "steps": steps, "warmup": warm,
+        "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u64" if field == "gl64" else "u32", "data": "synthetic (splitmix64 uniform residues)",
+        "config": {"workload": args.workload, "n": n, "field": field, "host_threads": threads},
+        "cpu_baseline": {"value": val, "unit": "Gelem/s", "cores": threads, "kind": kind, "sample": sample},
+        "e2e": {"value": val, "unit": "Gelem/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------- our arm
+def cpu_baseline(field: str, lg: int):
+    """One forward+inverse of the same size on one host core (oracle port)."""
+    import oracle as O
+
+    n = 1 << lg
+    if field == "gl64":
+        x = O.uniform_u64(3, n)
+        t0 = time.perf_counter()
+        y = O.ntt_gl64(x)
+        O.ntt_gl64(y, inverse=True)
+    else:
+        root, p = O.find_params(n, 11)
+        x = O.uniform_u32(3, p, n)
+        t0 = time.perf_counter()
+        y = O.ntt_u32(x, root, p)
+        O.ntt_u32(y, root, p, inverse=True)
+    dt = time.perf_counter() - t0
+    return {"value": 2 * n / dt / 1e9, "unit": "Gelem/s", "cores": 1, "kind": "port",
+            "sample": f"one {field} 2^{lg} forward+inverse on one host core ({dt:.1f} s), oracle restatement of "
+                      "the reference Stockham loop (src/ntt/ntt_cpu.cpp:46-85)"}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    rank, world, local = dist_env()
+    import torch
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+    import stntt_gb300 as st
+
+    field, lg = WORKLOADS[args.workload]
+    n = 1 << lg
+    esz = 8 if field == "gl64" else 4
+    ctx = st.Context(local)
+    stream = torch.cuda.Stream(device=dev)
+    sp = stream.cuda_stream
+    if field == "gl64":
+        data = torch.empty(n, dtype=torch.int64, device=dev)
+        st.fill_uniform_gl64(data, 1234 + rank, stream=sp)
+        fwd = lambda: ctx.ntt_gl64(data, lg, 1, inverse=False, stream=sp)  # noqa: E731
+        inv = lambda: ctx.ntt_gl64(data, lg, 1, inverse=True, stream=sp)  # noqa: E731
+        fid, p, root = st.FIELD_GL64, 0, 0
+    else:
+        p, root = st.params_u32(lg)
+        data = torch.empty(n, dtype=torch.int32, device=dev)
+        st.fill_uniform_u32(data, 1234 + rank, p, stream=sp)
+        fwd = lambda: ctx.ntt_u32(data, lg, 1, p, root, inverse=False, stream=sp)  # noqa: E731
+        inv = lambda: ctx.ntt_u32(data, lg, 1, p, root, inverse=True, stream=sp)  # noqa: E731
+        fid = st.FIELD_U32
+    passes, pass_logs = ctx.plan_info(fid, lg, p, root)
+    stream.synchronize()
+    ref_copy = data.clone()
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.int32, device=dev)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            fwd()
+            inv()
+        stream.synchronize()
+        ok = bool(torch.equal(data, ref_copy))  # forward+inverse is the identity
+
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+               torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        sampler = ClockSampler(int(os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[0])
+                               if os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0].isdigit() else local)
+        sampler.start()
+        time.sleep(0.25)
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        for i in range(args.steps):
+            flush.zero_()  # L2 flush, outside the events
+            a, b, c = ev[i]
+            a.record(stream)
+            fwd()
+            b.record(stream)
+            inv()
+            c.record(stream)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        clocks = sampler.stop()
+    t_fwd = [ev[i][0].elapsed_time(ev[i][1]) for i in range(args.steps)]
+    t_inv = [ev[i][1].elapsed_time(ev[i][2]) for i in range(args.steps)]
+    step_ms = float(np.sum(t_fwd) + np.sum(t_inv)) / args.steps
+    total_ms = step_ms * args.steps
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+        step_ms = total_ms / args.steps
+    value = world * 2 * n * args.steps / (total_ms / 1e3) / 1e9
+
+    # roofline of the tile kernel: B_alg per launch = 2 n w (one read + one write)
+    hbm, hbm_kind = peaks()
+    launch_ms = (float(np.mean(t_fwd)) + float(np.mean(t_inv))) / 2 / passes
+    bytes_per_launch = 2 * n * esz
+    achieved = bytes_per_launch / (launch_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                "traffic": None, "peak_kind": hbm_kind,
+                "bytes_per_launch": bytes_per_launch, "launches_per_transform": passes,
+                "pass_log_lengths": pass_logs, "mean_launch_us": launch_ms * 1e3,
+                "b_alg_per_transform": passes * bytes_per_launch if passes > 1 else 2 * n * esz,
+                "min_pass_floor_bytes": 2 * n * esz}
+
+    # end to end through the C-ABI host-buffer call (pinned host memory)
+    e2e = None
+    if not args.no_e2e and field == "gl64":
+        host = torch.empty(n, dtype=torch.int64, pin_memory=True)
+        host.copy_(ref_copy.cpu())
+        hv = host.numpy().view(np.uint64)
+        ctx.ntt_gl64_host(hv, lg)
+        ctx.ntt_gl64_host(hv, lg, inverse=True)
+        k = max(3, min(args.steps, 50))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(k):
+            ctx.ntt_gl64_host(hv, lg)
+            ctx.ntt_gl64_host(hv, lg, inverse=True)
+        dt = (time.perf_counter() - t0) / k
+        ok = ok and bool(torch.equal(host, ref_copy.cpu()))
+        e2e = {"value": world * 2 * n / dt / 1e9, "unit": "Gelem/s", "h2d_bytes_per_step": 2 * n * esz,
+               "d2h_bytes_per_step": 2 * n * esz, "ms_per_step": dt * 1e3,
+               "api": "stntt_ntt_gl64_host (forward, then inverse; each copies in and out)"}
+    elif not args.no_e2e:
+        host = torch.empty(n, dtype=torch.int32, pin_memory=True)
+        host.copy_(ref_copy.cpu())
+        k = max(3, min(args.steps, 50))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(k):
+            with torch.cuda.stream(stream):
+                data.copy_(host, non_blocking=True)
+                fwd()
+                inv()
+                host.copy_(data, non_blocking=True)
+            stream.synchronize()
+        dt = (time.perf_counter() - t0) / k
+        e2e = {"value": world * 2 * n / dt / 1e9, "unit": "Gelem/s", "h2d_bytes_per_step": n * esz,
+               "d2h_bytes_per_step": n * esz, "ms_per_step": dt * 1e3,
+               "api": "pinned H2D + stntt_ntt_u32 forward + inverse + D2H"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(field, lg)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC if args.workload == DEFAULT_WORKLOAD else f"NTT Gelem/s ({args.workload})",
+            "value": value, "unit": "Gelem/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u64" if field == "gl64" else "u32",
+            "data": "synthetic (splitmix64 uniform residues in [0,p), generated on the device)",
+            "config": {"workload": args.workload, "field": field, "n": n, "batch": 1,
+                       "step": "forward + inverse, in place", "l2": "flushed between steps (256 MiB write)",
+                       "parallelism": f"replicas x{world}"},
+            "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
+            "gpu_launches": 2 * passes * args.steps, "round_trip_ok": ok,
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

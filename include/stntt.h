@@ -1,0 +1,168 @@
+/*
+ * stntt.h -- C ABI of the GB300-native stNTT library (libstntt.so).
+ *
+ * Number-theoretic transforms on one NVIDIA GB300 (sm_103a), natural order in
+ * and out, over two fields:
+ *   - the reference's per-size 32-bit prime: p = k*n + 1 (the smallest such
+ *     prime >= min_mod) with root g^((p-1)/n), g the smallest generator
+ *     (findParams, src/ntt/ntt_util.cpp:10-49); any prime p < 2^31 with a
+ *     primitive n-th root is accepted;
+ *   - Goldilocks, p = 2^64 - 2^32 + 1, root 7^((p-1)/n).
+ *
+ * Conventions
+ *   - Forward:  X[k] = sum_j x[j] * root^(j*k) mod p        (nttStockham)
+ *   - Inverse:  x[j] = n^-1 * sum_k X[k] * root^(-j*k) mod p
+ *   - Device-pointer calls are asynchronous on the caller's stream
+ *     (a cudaStream_t passed as `stream`; NULL = legacy default stream).
+ *   - The caller owns every data buffer. A context owns its twiddle tables,
+ *     plans and per-stream workspaces. Every function returns a status and
+ *     never exits the process; stntt_last_error() gives the message.
+ *   - The first call for a given (field, size, root, direction) builds its
+ *     twiddle tables and synchronises an internal stream: make that first
+ *     call (or stntt_prepare) before capturing a stream into a CUDA graph.
+ *   - Input residues must be canonical (< p) unless stated otherwise.
+ *
+ * Thread safety: one context may be shared by several host threads (its caches
+ * are locked); calls on different streams use different workspaces.
+ */
+#ifndef STNTT_H
+#define STNTT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define STNTT_VERSION 1
+
+typedef enum stntt_status {
+    STNTT_OK = 0,
+    STNTT_EINVAL = 1,       /* bad argument (reference: std::invalid_argument) */
+    STNTT_ENOMEM = 2,       /* device or host allocation failed */
+    STNTT_ECUDA = 3,        /* a CUDA runtime call failed (reference: CCErr -> exit) */
+    STNTT_ETIMEOUT = 4,     /* a bounded device-side wait gave up */
+    STNTT_EUNSUPPORTED = 5, /* size / field combination outside the supported range */
+} stntt_status;
+
+typedef enum stntt_dir { STNTT_FORWARD = 0, STNTT_INVERSE = 1 } stntt_dir;
+typedef enum stntt_field { STNTT_FIELD_U32 = 0, STNTT_FIELD_GL64 = 1 } stntt_field;
+
+/* flags for the 32-bit field */
+#define STNTT_FLAG_REF_WRAP 0x1u /* reproduce the reference's int32 wrap-around arithmetic
+                                    (forward only; equals the reference CPU bit for bit) */
+
+typedef struct stntt_ctx stntt_ctx;
+typedef void *stntt_stream; /* a cudaStream_t */
+
+/* ---- context -------------------------------------------------------------- */
+/* Replaces the reference's process-global device state (__constant__ twiddles
+ * and global_twiddles, src/cuda/ntt/implementations/common.cuh:7-9). */
+int stntt_init(stntt_ctx **ctx, int device);
+int stntt_destroy(stntt_ctx *ctx);
+const char *stntt_last_error(const stntt_ctx *ctx);
+const char *stntt_status_string(int status);
+int stntt_version(void);
+/* Bytes of device memory the context currently holds (tables + workspaces). */
+int stntt_mem_usage(const stntt_ctx *ctx, size_t *bytes);
+
+/* ---- parameters ------------------------------------------------------------- */
+/* findParams(size, min_mod) -> (root, mod): src/ntt/ntt_util.cpp:10-14
+ * (findModulus :16-27, findPrimitiveRoot :29-34, findGenerator :36-42). */
+int stntt_find_params(uint64_t size, uint64_t min_mod, uint64_t *root, uint64_t *mod);
+/* findParams(2^log_n, 11), the call every reference caller makes
+ * (src/main.cu:37, src/bench.cu:35, src/tests/cuda/ntt/st_ntt_test.cu:20). */
+int stntt_params_u32(uint32_t log_n, uint32_t *p, uint32_t *root);
+/* Goldilocks root of unity of order 2^log_n (log_n <= 32): 7^((p-1)/2^log_n). */
+int stntt_gl64_root(uint32_t log_n, uint64_t *root);
+
+/* Build (or look up) the twiddle tables and plan for a transform, on an
+ * internal stream, and wait for them. Optional: the transform calls do it on
+ * first use. For STNTT_FIELD_GL64, p and root are ignored. */
+int stntt_prepare(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t p, uint32_t root, int dir);
+
+/* Shape of the plan stntt_prepare builds: the number of HBM passes (kernel
+ * launches per transform) and log2 of each pass's tile length (up to 4). */
+int stntt_plan_info(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t p, uint32_t root, int dir,
+                    uint32_t *passes, uint32_t *pass_logs);
+
+/* ---- transforms on device buffers ------------------------------------------ */
+/* In place, `batch` contiguous transforms of 2^log_n elements.
+ * Replaces cuda::ntt::autoNtt<n>(NttArgs) (src/cuda/ntt/ntt_kernel.cuh:153-200)
+ * and the kernels it launches (stNttRadix2, stNttRadix2Adaptive,
+ * sttNttGlobalRadix2). Supported: log_n in [0, 27] with p < 2^31.
+ * flags: STNTT_FLAG_REF_WRAP (dir must be STNTT_FORWARD). */
+int stntt_ntt_u32(stntt_ctx *ctx, uint32_t *d_data, uint32_t log_n, uint32_t batch, uint32_t p, uint32_t root,
+                  int dir, uint32_t flags, stntt_stream stream);
+/* Goldilocks, in place. The Goldilocks driver sttNttGoldilocks
+ * (src/cuda/ntt/implementations/st_ntt_goldilocks.cuh:198-225) is a
+ * non-functional scaffold in the reference; this is its working counterpart.
+ * Supported: log_n in [0, 32]. */
+int stntt_ntt_gl64(stntt_ctx *ctx, uint64_t *d_data, uint32_t log_n, uint32_t batch, int dir, stntt_stream stream);
+/* Out-of-place variants: d_in is not modified (may equal d_out). */
+int stntt_ntt_u32_oop(stntt_ctx *ctx, const uint32_t *d_in, uint32_t *d_out, uint32_t log_n, uint32_t batch,
+                      uint32_t p, uint32_t root, int dir, stntt_stream stream);
+int stntt_ntt_gl64_oop(stntt_ctx *ctx, const uint64_t *d_in, uint64_t *d_out, uint32_t log_n, uint32_t batch,
+                       int dir, stntt_stream stream);
+/* The first `nsteps` radix-2 Stockham stages only (nsteps <= log_n), the
+ * reference's std::optional<int> nsteps hook (src/ntt/ntt_cpu.h:8). A debug
+ * path: one launch per stage. flags as for stntt_ntt_u32. */
+int stntt_ntt_u32_steps(stntt_ctx *ctx, uint32_t *d_data, uint32_t log_n, uint32_t batch, uint32_t p,
+                        uint32_t root, uint32_t nsteps, uint32_t flags, stntt_stream stream);
+
+/* ---- host-buffer convenience (copies in, transforms, copies out; synchronous) */
+/* Mirrors nttStockham(int *vec, int size, int root, int mod, nsteps) and its
+ * batched overload (src/ntt/ntt_cpu.h:8-9, ntt_cpu.cpp:46-90): in place on a
+ * host int array. nsteps < 0 means all stages. Without STNTT_FLAG_REF_WRAP the
+ * result is the exact field NTT (equal to the reference for n <= 2^13); with
+ * it, equal to the reference at every n. */
+int stntt_ntt_stockham_host(stntt_ctx *ctx, int32_t *vec, int32_t size, int32_t root, int32_t mod,
+                            int32_t batches, int32_t nsteps, uint32_t flags);
+int stntt_ntt_gl64_host(stntt_ctx *ctx, uint64_t *vec, uint32_t log_n, uint32_t batch, int dir);
+
+/* ---- uneven batches ----------------------------------------------------------- */
+typedef struct stntt_job {
+    uint32_t field; /* stntt_field */
+    uint32_t log_n;
+    uint32_t dir;   /* stntt_dir */
+    uint32_t p;     /* STNTT_FIELD_U32 only */
+    uint32_t root;  /* STNTT_FIELD_U32 only */
+    uint32_t reserved;
+    void *data;     /* device pointer, 2^log_n elements, transformed in place */
+} stntt_job;
+
+/* Many independent transforms of uneven sizes, fields and directions in one
+ * persistent launch (plus one launch for the few jobs too large for it).
+ * Extends the reference's uniform `batches` packing
+ * (src/cuda/ntt/ntt_kernel.cuh:31-39). */
+int stntt_ntt_batch(stntt_ctx *ctx, const stntt_job *jobs, size_t njobs, stntt_stream stream);
+/* Same jobs, one launch sequence per job (the comparison baseline). */
+int stntt_ntt_batch_per_call(stntt_ctx *ctx, const stntt_job *jobs, size_t njobs, stntt_stream stream);
+
+/* ---- polynomial multiplication (pwcNtt / pwc_convolution, ntt_cpu.cpp:167-193) */
+/* d_out = cyclic convolution of d_a and d_b, length 2^log_n, i.e. the product
+ * a*b mod (x^n - 1); equal to the plain product when deg a + deg b < n.
+ * d_out may alias d_a or d_b. */
+int stntt_polymul_u32(stntt_ctx *ctx, const uint32_t *d_a, const uint32_t *d_b, uint32_t *d_out, uint32_t log_n,
+                      uint32_t p, uint32_t root, stntt_stream stream);
+int stntt_polymul_gl64(stntt_ctx *ctx, const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_out, uint32_t log_n,
+                       stntt_stream stream);
+/* d_out[i] = d_a[i] * d_b[i] mod p (elemWiseMul, src/ntt/ntt_util.h:29-33). */
+int stntt_pointwise_mul_u32(const uint32_t *d_a, const uint32_t *d_b, uint32_t *d_out, size_t count, uint32_t p,
+                            stntt_stream stream);
+int stntt_pointwise_mul_gl64(const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_out, size_t count,
+                             stntt_stream stream);
+
+/* ---- synthetic inputs ------------------------------------------------------------ */
+/* Uniform residues in [0,p) from a counter-based splitmix64 stream:
+ * element i, attempt a: z = mix64(seed + 0x9E3779B97F4A7C15 * (i + (a << 40) + 1));
+ * u32 accepts (z >> 32) below the largest multiple of p and returns it mod p;
+ * gl64 accepts z < p. */
+int stntt_fill_uniform_u32(uint32_t *d_out, size_t count, uint64_t seed, uint32_t p, stntt_stream stream);
+int stntt_fill_uniform_gl64(uint64_t *d_out, size_t count, uint64_t seed, stntt_stream stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* STNTT_H */

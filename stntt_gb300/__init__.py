@@ -1,0 +1,330 @@
+"""stntt_gb300 -- GB300-native number-theoretic transforms (Python host side).
+
+This package is a thin ctypes layer over ``libstntt.so`` (the CUDA library in
+``csrc/``, C ABI in ``include/stntt.h``). It mirrors the reference's host
+interface for the hot path (AlvaroPardoFente/stNTT, ``src/ntt``):
+
+* ``findParams(size, min_mod)`` -> ``(root, mod)``  (src/ntt/ntt_util.cpp:10)
+* ``nttStockham(vec, size, root, mod, batches=1, nsteps=None)`` -- in place on a
+  host int32 array, natural order in and out (src/ntt/ntt_cpu.cpp:46-90); the
+  transform runs on the GPU. ``ref_wrap=True`` reproduces the reference's
+  int32 wrap-around arithmetic bit for bit.
+* ``Context`` -- device-buffer transforms on torch tensors, asynchronous on the
+  current CUDA stream (replaces ``cuda::ntt::autoNtt<n>``,
+  src/cuda/ntt/ntt_kernel.cuh:153-200).
+
+There is no CPU fallback: every entry point raises ``StnttError`` when the
+CUDA library is missing or fails.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import platform
+from pathlib import Path
+from typing import Iterable, Optional, Sequence
+
+import numpy as np
+
+__all__ = [
+    "StnttError", "lib", "Context", "findParams", "params_u32", "gl64_root", "nttStockham",
+    "GL_P", "FORWARD", "INVERSE", "FIELD_U32", "FIELD_GL64", "FLAG_REF_WRAP", "Job",
+]
+
+PKG = Path(__file__).resolve().parent
+SO_PATH = PKG / "_lib" / platform.machine() / "libstntt.so"
+GL_P = 0xFFFFFFFF00000001
+FORWARD, INVERSE = 0, 1
+FIELD_U32, FIELD_GL64 = 0, 1
+FLAG_REF_WRAP = 0x1
+STATUS = {0: "OK", 1: "EINVAL", 2: "ENOMEM", 3: "ECUDA", 4: "ETIMEOUT", 5: "EUNSUPPORTED"}
+
+
+class StnttError(RuntimeError):
+    def __init__(self, status: int, msg: str = ""):
+        self.status = status
+        super().__init__(f"stntt {STATUS.get(status, status)}: {msg}")
+
+
+class Job(C.Structure):
+    """``stntt_job`` (include/stntt.h)."""
+
+    _fields_ = [("field", C.c_uint32), ("log_n", C.c_uint32), ("dir", C.c_uint32), ("p", C.c_uint32),
+                ("root", C.c_uint32), ("reserved", C.c_uint32), ("data", C.c_void_p)]
+
+
+_LIB = None
+_vp, _u32, _u64, _i32, _sz, _int = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int32, C.c_size_t, C.c_int
+
+_SIGS = {
+    "stntt_version": (_int, []),
+    "stntt_status_string": (C.c_char_p, [_int]),
+    "stntt_init": (_int, [C.POINTER(_vp), _int]),
+    "stntt_destroy": (_int, [_vp]),
+    "stntt_last_error": (C.c_char_p, [_vp]),
+    "stntt_mem_usage": (_int, [_vp, C.POINTER(_sz)]),
+    "stntt_find_params": (_int, [_u64, _u64, C.POINTER(_u64), C.POINTER(_u64)]),
+    "stntt_params_u32": (_int, [_u32, C.POINTER(_u32), C.POINTER(_u32)]),
+    "stntt_gl64_root": (_int, [_u32, C.POINTER(_u64)]),
+    "stntt_prepare": (_int, [_vp, _int, _u32, _u32, _u32, _int]),
+    "stntt_plan_info": (_int, [_vp, _int, _u32, _u32, _u32, _int, C.POINTER(_u32), C.POINTER(_u32)]),
+    "stntt_ntt_u32": (_int, [_vp, _vp, _u32, _u32, _u32, _u32, _int, _u32, _vp]),
+    "stntt_ntt_gl64": (_int, [_vp, _vp, _u32, _u32, _int, _vp]),
+    "stntt_ntt_u32_oop": (_int, [_vp, _vp, _vp, _u32, _u32, _u32, _u32, _int, _vp]),
+    "stntt_ntt_gl64_oop": (_int, [_vp, _vp, _vp, _u32, _u32, _int, _vp]),
+    "stntt_ntt_u32_steps": (_int, [_vp, _vp, _u32, _u32, _u32, _u32, _u32, _u32, _vp]),
+    "stntt_ntt_stockham_host": (_int, [_vp, _vp, _i32, _i32, _i32, _i32, _i32, _u32]),
+    "stntt_ntt_gl64_host": (_int, [_vp, _vp, _u32, _u32, _int]),
+    "stntt_ntt_batch": (_int, [_vp, C.POINTER(Job), _sz, _vp]),
+    "stntt_ntt_batch_per_call": (_int, [_vp, C.POINTER(Job), _sz, _vp]),
+    "stntt_polymul_u32": (_int, [_vp, _vp, _vp, _vp, _u32, _u32, _u32, _vp]),
+    "stntt_polymul_gl64": (_int, [_vp, _vp, _vp, _vp, _u32, _vp]),
+    "stntt_pointwise_mul_u32": (_int, [_vp, _vp, _vp, _sz, _u32, _vp]),
+    "stntt_pointwise_mul_gl64": (_int, [_vp, _vp, _vp, _sz, _vp]),
+    "stntt_fill_uniform_u32": (_int, [_vp, _sz, _u64, _u32, _vp]),
+    "stntt_fill_uniform_gl64": (_int, [_vp, _sz, _u64, _vp]),
+}
+
+
+def header_symbols() -> list[str]:
+    """Every function name declared in include/stntt.h."""
+    import re
+
+    hdr = (PKG.parent / "include" / "stntt.h").read_text()
+    return sorted(set(re.findall(r"^\s*(?:int|const char \*)\s*(stntt_\w+)\s*\(", hdr, re.M)))
+
+
+def lib() -> C.CDLL:
+    """Load libstntt.so; raises StnttError when it has not been built."""
+    global _LIB
+    if _LIB is None:
+        if not SO_PATH.exists():
+            raise StnttError(3, f"{SO_PATH} is missing: build it with __graft_entry__.build() "
+                                "(there is no CPU fallback)")
+        L = C.CDLL(str(SO_PATH))
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+def _check(rc: int, ctx: Optional[int] = None) -> None:
+    if rc != 0:
+        msg = ""
+        if ctx:
+            raw = lib().stntt_last_error(ctx)
+            msg = raw.decode() if raw else ""
+        raise StnttError(rc, msg)
+
+
+# ---------------------------------------------------------------- parameters
+def findParams(size: int, min_mod: int = 11) -> tuple[int, int]:
+    """findParams(size, min_mod) -> (root, mod), src/ntt/ntt_util.cpp:10-14."""
+    r, m = _u64(), _u64()
+    _check(lib().stntt_find_params(size, min_mod, C.byref(r), C.byref(m)))
+    return r.value, m.value
+
+
+def params_u32(log_n: int) -> tuple[int, int]:
+    """(p, root) = findParams(2^log_n, 11) as the reference's callers use it."""
+    p, r = _u32(), _u32()
+    _check(lib().stntt_params_u32(log_n, C.byref(p), C.byref(r)))
+    return p.value, r.value
+
+
+def gl64_root(log_n: int) -> int:
+    r = _u64()
+    _check(lib().stntt_gl64_root(log_n, C.byref(r)))
+    return r.value
+
+
+def _log2(n: int) -> int:
+    if n <= 0 or n & (n - 1):
+        raise StnttError(1, f"size ({n}) must be a power of 2")
+    return n.bit_length() - 1
+
+
+# ---------------------------------------------------------------- context
+_DEFAULT: dict[int, "Context"] = {}
+
+
+def _ptr(t) -> int:
+    """Device pointer of a torch tensor (or a raw int)."""
+    if isinstance(t, int):
+        return t
+    if not t.is_cuda:
+        raise StnttError(1, "tensor must live on a CUDA device")
+    if not t.is_contiguous():
+        raise StnttError(1, "tensor must be contiguous")
+    return t.data_ptr()
+
+
+def _stream(stream) -> int:
+    if stream is None:
+        import torch
+
+        return torch.cuda.current_stream().cuda_stream
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream
+
+
+class Context:
+    """A ``stntt_ctx``: twiddle tables, plans and workspaces on one device."""
+
+    def __init__(self, device: int = 0):
+        h = _vp()
+        _check(lib().stntt_init(C.byref(h), device))
+        self._h = h.value
+        self.device = device
+
+    @classmethod
+    def default(cls, device: int = 0) -> "Context":
+        if device not in _DEFAULT:
+            _DEFAULT[device] = cls(device)
+        return _DEFAULT[device]
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().stntt_destroy(self._h)
+            self._h = None
+
+    def __del__(self):  # pragma: no cover - interpreter shutdown order
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self) -> int:
+        return self._h
+
+    def mem_usage(self) -> int:
+        b = _sz()
+        _check(lib().stntt_mem_usage(self._h, C.byref(b)), self._h)
+        return b.value
+
+    def prepare(self, field: int, log_n: int, p: int = 0, root: int = 0, inverse: bool = False) -> None:
+        _check(lib().stntt_prepare(self._h, field, log_n, p, root, INVERSE if inverse else FORWARD), self._h)
+
+    def plan_info(self, field: int, log_n: int, p: int = 0, root: int = 0, inverse: bool = False):
+        """(number of HBM passes, [log2 tile length per pass])."""
+        n = _u32()
+        logs = (_u32 * 4)()
+        _check(lib().stntt_plan_info(self._h, field, log_n, p, root, INVERSE if inverse else FORWARD,
+                                     C.byref(n), logs), self._h)
+        return n.value, list(logs)[: n.value]
+
+    # -- device transforms (torch tensors: int32 storage for u32, int64 for gl64)
+    def ntt_u32(self, data, log_n: int, batch: int, p: int, root: int, inverse: bool = False,
+                ref_wrap: bool = False, stream=None) -> None:
+        flags = FLAG_REF_WRAP if ref_wrap else 0
+        _check(lib().stntt_ntt_u32(self._h, _ptr(data), log_n, batch, p, root, INVERSE if inverse else FORWARD,
+                                   flags, _stream(stream)), self._h)
+
+    def ntt_u32_oop(self, src, dst, log_n: int, batch: int, p: int, root: int, inverse: bool = False,
+                    stream=None) -> None:
+        _check(lib().stntt_ntt_u32_oop(self._h, _ptr(src), _ptr(dst), log_n, batch, p, root,
+                                       INVERSE if inverse else FORWARD, _stream(stream)), self._h)
+
+    def ntt_u32_steps(self, data, log_n: int, batch: int, p: int, root: int, nsteps: int,
+                      ref_wrap: bool = False, stream=None) -> None:
+        _check(lib().stntt_ntt_u32_steps(self._h, _ptr(data), log_n, batch, p, root, nsteps,
+                                         FLAG_REF_WRAP if ref_wrap else 0, _stream(stream)), self._h)
+
+    def ntt_gl64(self, data, log_n: int, batch: int = 1, inverse: bool = False, stream=None) -> None:
+        _check(lib().stntt_ntt_gl64(self._h, _ptr(data), log_n, batch, INVERSE if inverse else FORWARD,
+                                    _stream(stream)), self._h)
+
+    def ntt_gl64_oop(self, src, dst, log_n: int, batch: int = 1, inverse: bool = False, stream=None) -> None:
+        _check(lib().stntt_ntt_gl64_oop(self._h, _ptr(src), _ptr(dst), log_n, batch,
+                                        INVERSE if inverse else FORWARD, _stream(stream)), self._h)
+
+    def polymul_u32(self, a, b, out, log_n: int, p: int, root: int, stream=None) -> None:
+        _check(lib().stntt_polymul_u32(self._h, _ptr(a), _ptr(b), _ptr(out), log_n, p, root, _stream(stream)),
+               self._h)
+
+    def polymul_gl64(self, a, b, out, log_n: int, stream=None) -> None:
+        _check(lib().stntt_polymul_gl64(self._h, _ptr(a), _ptr(b), _ptr(out), log_n, _stream(stream)), self._h)
+
+    def ntt_batch(self, jobs: Sequence[Job], per_call: bool = False, stream=None) -> None:
+        arr = (Job * len(jobs))(*jobs)
+        f = lib().stntt_ntt_batch_per_call if per_call else lib().stntt_ntt_batch
+        _check(f(self._h, arr, len(jobs), _stream(stream)), self._h)
+
+    # -- host arrays (synchronous)
+    def ntt_stockham_host(self, vec: np.ndarray, size: int, root: int, mod: int, batches: int = 1,
+                          nsteps: Optional[int] = None, ref_wrap: bool = False) -> np.ndarray:
+        if vec.dtype != np.int32 or not vec.flags.c_contiguous:
+            raise StnttError(1, "vec must be a C-contiguous int32 array")
+        if vec.size < size * batches:
+            raise StnttError(1, "vec is shorter than size * batches")
+        _check(lib().stntt_ntt_stockham_host(self._h, vec.ctypes.data, size, root, mod, batches,
+                                             -1 if nsteps is None else nsteps,
+                                             FLAG_REF_WRAP if ref_wrap else 0), self._h)
+        return vec
+
+    def ntt_gl64_host(self, vec: np.ndarray, log_n: int, batch: int = 1, inverse: bool = False) -> np.ndarray:
+        if vec.dtype != np.uint64 or not vec.flags.c_contiguous:
+            raise StnttError(1, "vec must be a C-contiguous uint64 array")
+        _check(lib().stntt_ntt_gl64_host(self._h, vec.ctypes.data, log_n, batch, INVERSE if inverse else FORWARD),
+               self._h)
+        return vec
+
+
+def nttStockham(vec: np.ndarray, size: int, root: int, mod: int, batches: int = 1,
+                nsteps: Optional[int] = None, ref_wrap: bool = False, device: int = 0) -> np.ndarray:
+    """In-place forward NTT of a host int32 array on the GPU.
+
+    Mirrors ``nttStockham(int *vec, int size, int root, int mod, nsteps)`` and
+    ``nttStockham(std::span<int>, size, root, mod, batches, nsteps)``
+    (src/ntt/ntt_cpu.h:8-9). Raises ``StnttError`` (EINVAL, "size (N) must be a
+    power of 2") where the reference throws ``std::invalid_argument``.
+    """
+    return Context.default(device).ntt_stockham_host(vec, size, root, mod, batches, nsteps, ref_wrap)
+
+
+# ---------------------------------------------------------------- inputs
+def fill_uniform_u32(t, seed: int, p: int, stream=None) -> None:
+    """Device-side uniform residues in [0, p) (counter-based splitmix64)."""
+    _check(lib().stntt_fill_uniform_u32(_ptr(t), t.numel(), seed, p, _stream(stream)))
+
+
+def fill_uniform_gl64(t, seed: int, stream=None) -> None:
+    _check(lib().stntt_fill_uniform_gl64(_ptr(t), t.numel(), seed, _stream(stream)))
+
+
+def uniform_u32_host(seed: int, p: int, n: int) -> np.ndarray:
+    """Host copy of the same generator (numpy), for end-to-end host inputs."""
+    return _uniform_host(seed, n, p, bits32=True).astype(np.uint32)
+
+
+def uniform_gl64_host(seed: int, n: int) -> np.ndarray:
+    return _uniform_host(seed, n, GL_P, bits32=False)
+
+
+def _mix(z: np.ndarray) -> np.ndarray:
+    z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return z ^ (z >> np.uint64(31))
+
+
+def _uniform_host(seed: int, n: int, p: int, bits32: bool) -> np.ndarray:
+    with np.errstate(over="ignore"):
+        out = np.empty(n, np.uint64)
+        todo = np.arange(n, dtype=np.uint64)
+        attempt = 0
+        limit = (1 << 32) - ((1 << 32) % p) if bits32 else p
+        while todo.size:
+            ctr = todo + np.uint64(attempt << 40) + np.uint64(1)
+            z = _mix(np.uint64(seed) + np.uint64(0x9E3779B97F4A7C15) * ctr)
+            if bits32:
+                z = z >> np.uint64(32)
+            ok = z < np.uint64(limit)
+            vals = z[ok] % np.uint64(p) if bits32 else z[ok]
+            out[todo[ok]] = vals
+            todo = todo[~ok]
+            attempt += 1
+        return out

@@ -1,0 +1,1007 @@
+// api.cu -- host side of libstntt: parameters, plans, twiddle cache,
+// workspaces and the C ABI declared in include/stntt.h.
+//
+// Reference boundary this replaces: cuda::ntt::NttArgs / getNttKernelArgs /
+// autoNtt<n> (src/cuda/ntt/ntt_kernel.cuh:31-200), which allocate, upload a
+// freshly built twiddle table (initTwiddles, .../implementations/common.cuh:
+// 17-109) and launch on every call, and exit the process on CUDA errors
+// (CCErr, src/cuda/cu_util.cuh:12-28). Here a context caches device-built
+// twiddle tables and plans, runs asynchronously on the caller's stream and
+// returns a status.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/stntt.h"
+#include "internal.h"
+
+namespace stntt {
+
+cudaError_t launch_tile_u32(const PassDesc &, uint32_t, const void *, const void *, void *, uint64_t, cudaStream_t);
+cudaError_t launch_tile_gl64(const PassDesc &, uint32_t, const void *, const void *, void *, uint64_t,
+                             cudaStream_t);
+cudaError_t gen_powers_u32(void *, uint64_t, uint64_t, uint64_t, uint32_t, cudaStream_t);
+cudaError_t gen_powers_gl64(void *, uint64_t, uint64_t, uint64_t, cudaStream_t);
+cudaError_t pointwise_u32(const void *, const void *, void *, size_t, uint32_t, cudaStream_t);
+cudaError_t pointwise_gl64(const void *, const void *, void *, size_t, cudaStream_t);
+cudaError_t fill_uniform_u32(void *, size_t, uint64_t, uint32_t, cudaStream_t);
+cudaError_t fill_uniform_gl64(void *, size_t, uint64_t, cudaStream_t);
+cudaError_t copy_scale_u32(const void *, void *, size_t, uint64_t, uint32_t, cudaStream_t);
+cudaError_t copy_scale_gl64(const void *, void *, size_t, uint64_t, cudaStream_t);
+
+static constexpr uint64_t GL_P = 0xFFFFFFFF00000001ull;
+typedef unsigned __int128 u128;
+
+uint64_t host_pow_mod(uint64_t b, uint64_t e, uint64_t m) {
+    uint64_t r = 1 % m;
+    b %= m;
+    while (e) {
+        if (e & 1)
+            r = (uint64_t)((u128)r * b % m);
+        b = (uint64_t)((u128)b * b % m);
+        e >>= 1;
+    }
+    return r;
+}
+uint64_t host_gl_mul(uint64_t a, uint64_t b) { return (uint64_t)((u128)a * b % GL_P); }
+uint64_t host_gl_pow(uint64_t b, uint64_t e) { return host_pow_mod(b, e, GL_P); }
+uint64_t host_tw_entry(int field, uint64_t w, uint32_t p) {
+    if (field == kFieldGL)
+        return w;
+    const uint64_t wp = (w << 32) / p;  // Shoup companion floor(w * 2^32 / p)
+    return (w & 0xffffffffull) | (wp << 32);
+}
+
+cudaError_t launch_tile(int field, const PassDesc &d, uint32_t p, const void *tables, const void *in, void *out,
+                        uint64_t batch, cudaStream_t s) {
+    return field == kFieldGL ? launch_tile_gl64(d, p, tables, in, out, batch, s)
+                             : launch_tile_u32(d, p, tables, in, out, batch, s);
+}
+cudaError_t launch_gen_powers(int field, void *out, uint64_t count, uint64_t base, uint64_t scale, uint32_t p,
+                              cudaStream_t s) {
+    return field == kFieldGL ? gen_powers_gl64(out, count, base, scale, s)
+                             : gen_powers_u32(out, count, base, scale, p, s);
+}
+cudaError_t launch_pointwise(int field, const void *a, const void *b, void *out, size_t count, uint32_t p,
+                             cudaStream_t s) {
+    return field == kFieldGL ? pointwise_gl64(a, b, out, count, s) : pointwise_u32(a, b, out, count, p, s);
+}
+cudaError_t launch_fill_uniform(int field, void *out, size_t count, uint64_t seed, uint32_t p, cudaStream_t s) {
+    return field == kFieldGL ? fill_uniform_gl64(out, count, seed, s) : fill_uniform_u32(out, count, seed, p, s);
+}
+cudaError_t launch_copy_scale(int field, const void *in, void *out, size_t count, uint64_t scale_tw, uint32_t p,
+                              cudaStream_t s) {
+    return field == kFieldGL ? copy_scale_gl64(in, out, count, scale_tw, s)
+                             : copy_scale_u32(in, out, count, scale_tw, p, s);
+}
+
+// ---------------------------------------------------------------------------
+// findParams (src/ntt/ntt_util.cpp:10-49): smallest prime mod = k*size + 1
+// >= min_mod (trial division), smallest generator g, root = g^((mod-1)/size).
+// ---------------------------------------------------------------------------
+static uint64_t isqrt_u64(uint64_t n) {
+    uint64_t r = 0;
+    for (uint64_t bit = 1ull << 31; bit; bit >>= 1) {
+        const uint64_t c = r | bit;
+        if (c <= n / c)
+            r = c;
+    }
+    return r;
+}
+static bool is_prime_td(uint64_t n) {
+    if (n < 2)
+        return n == 1;  // the reference's isPrime(1) is vacuously true; never reached (mod >= 2)
+    const uint64_t e = isqrt_u64(n);
+    for (uint64_t x = 2; x <= e; ++x)
+        if (n % x == 0)
+            return false;
+    return true;
+}
+static std::vector<uint64_t> prime_factors(uint64_t n) {
+    std::vector<uint64_t> f;
+    for (uint64_t i = 2; i <= isqrt_u64(n); ++i) {
+        if (n % i == 0) {
+            f.push_back(i);
+            while (n % i == 0)
+                n /= i;
+        }
+    }
+    if (n > 1)
+        f.push_back(n);
+    return f;
+}
+
+}  // namespace stntt
+
+using namespace stntt;
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+namespace {
+
+struct PlanKey {
+    int field;
+    uint32_t log_n, p;
+    uint64_t root;  // root of the direction (inverse: root^-1)
+    int dir;
+    bool operator<(const PlanKey &o) const {
+        return std::tie(field, log_n, p, root, dir) < std::tie(o.field, o.log_n, o.p, o.root, o.dir);
+    }
+};
+
+struct Plan {
+    int field = 0;
+    uint32_t log_n = 0, p = 0;
+    std::vector<PassDesc> passes;
+    void *d_tables = nullptr;
+    size_t table_bytes = 0;
+};
+
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+};
+
+}  // namespace
+
+struct stntt_ctx {
+    int device = 0;
+    std::mutex mu;
+    std::map<PlanKey, std::unique_ptr<Plan>> plans;
+    std::map<std::tuple<uint32_t, uint32_t, uint32_t, int>, DevBuf> stage_tables;  // (log_n, p, root, wrap)
+    std::map<cudaStream_t, DevBuf> workspaces;
+    cudaStream_t setup = nullptr;
+    // host-buffer calls: one at a time, on their own stream and staging buffer
+    std::mutex host_mu;
+    cudaStream_t host_stream = nullptr;
+    DevBuf host_stage;
+    std::string err;
+    size_t mem = 0;
+};
+
+namespace {
+
+int fail(stntt_ctx *ctx, int status, const std::string &msg) {
+    if (ctx) {
+        std::lock_guard<std::mutex> g(ctx->mu);
+        ctx->err = msg;
+    }
+    return status;
+}
+int cuda_fail(stntt_ctx *ctx, cudaError_t e, const char *what) {
+    return fail(ctx, STNTT_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+struct DeviceGuard {
+    int prev = -1;
+    cudaError_t err = cudaSuccess;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess)
+            prev = -1;
+        if (prev != dev)
+            err = cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        if (prev >= 0)
+            cudaSetDevice(prev);
+    }
+};
+
+uint32_t ilog2(uint64_t v) {
+    uint32_t l = 0;
+    while ((1ull << l) < v)
+        ++l;
+    return l;
+}
+
+// Field root of order 2^log_n for the given direction.
+uint64_t dir_root(int field, uint64_t root, uint32_t p, int dir) {
+    if (dir == STNTT_FORWARD)
+        return root;
+    return field == kFieldGL ? host_gl_pow(root, GL_P - 2) : host_pow_mod(root, p - 2, p);
+}
+uint64_t fpow(int field, uint64_t b, uint64_t e, uint32_t p) {
+    return field == kFieldGL ? host_gl_pow(b, e) : host_pow_mod(b, e, p);
+}
+uint64_t fmul(int field, uint64_t a, uint64_t b, uint32_t p) {
+    return field == kFieldGL ? host_gl_mul(a, b) : (uint64_t)((u128)a * b % p);
+}
+
+// Tile geometry for one pass: elements per thread E, columns per CTA C,
+// shared-memory column stride and size.
+void shape_pass(PassDesc &d, int field, uint64_t rows_per_transform, uint64_t col_limit) {
+    const uint32_t L = 1u << d.logL;
+    d.E = L < 16 ? L : (L >= 4096 ? 32 : 16);
+    const uint32_t U = L / d.E;
+    const uint32_t max_threads = d.E >= 32 ? 512 : 1024;
+    uint64_t C;
+    if (d.mode == kModeRow && d.logN == d.logL) {
+        C = std::max<uint64_t>(1, 256 / U);  // whole transforms per CTA: ~256 threads
+    } else {
+        C = std::min<uint64_t>(16, 16384 / L);
+    }
+    C = std::min<uint64_t>(C, max_threads / U);
+    C = std::min<uint64_t>(C, col_limit);
+    C = std::min<uint64_t>(C, 64);
+    C = std::max<uint64_t>(C, 1);
+    (void)rows_per_transform;
+    d.logC = ilog2(C);
+    d.threads = (uint32_t)(C * U);
+    const uint32_t padshift = field == kFieldGL ? 4 : 5;
+    const uint32_t banks = field == kFieldGL ? 16 : 32;
+    const uint32_t base = L + (L >> padshift);
+    uint32_t want;
+    if (d.tfast)
+        want = U < banks ? U : 0;
+    else
+        want = C < banks ? (uint32_t)(banks / C) : 0;
+    d.cs = base + ((want + banks - base % banks) % banks);
+    d.smem_bytes = (size_t)C * d.cs * (field == kFieldGL ? 8 : 4);
+}
+
+// Build the pass list and the twiddle tables for one transform.
+int build_plan(stntt_ctx *ctx, Plan &pl, int field, uint32_t log_n, uint32_t p, uint64_t root_dir, int dir) {
+    pl.field = field;
+    pl.log_n = log_n;
+    pl.p = p;
+    if (log_n == 0)
+        return STNTT_OK;
+    const uint64_t n = 1ull << log_n;
+    const uint32_t single_max = 13, tile_max = 12;
+    std::vector<uint32_t> logs;
+    if (log_n <= single_max) {
+        logs.push_back(log_n);
+    } else {
+        const uint32_t K = (log_n + tile_max - 1) / tile_max;
+        for (uint32_t i = 0; i < K; ++i)
+            logs.push_back(log_n / K + (i < log_n % K ? 1 : 0));
+    }
+    const uint32_t K = (uint32_t)logs.size();
+    struct TableReq {
+        uint64_t count, base, scale;
+    };
+    std::vector<TableReq> reqs;
+    uint64_t off = 0;
+    auto add_table = [&](uint64_t count, uint64_t base, uint64_t scale) {
+        reqs.push_back({count, base, scale});
+        const uint64_t o = off;
+        off += count;
+        return o;
+    };
+    const uint64_t modulus = field == kFieldGL ? GL_P : p;
+    const uint64_t ninv = dir == STNTT_INVERSE ? fpow(field, n % modulus, modulus - 2, p) : 1;  // n^-1
+    uint32_t done = 0;  // log2 of the product of the lengths of earlier passes
+    for (uint32_t i = 0; i < K; ++i) {
+        PassDesc d;
+        d.logL = logs[i];
+        d.logN = log_n;
+        const uint32_t L = 1u << d.logL;
+        const uint64_t wL = fpow(field, root_dir, n >> d.logL, p);  // w_L = w_n^(n/L)
+        d.tw_off = add_table(L, wL, 1);
+        // radix-16 internal roots (for L < 16: entry j*16/L = w_L^j)
+        if (L >= 16) {
+            const uint64_t w16 = fpow(field, wL, L / 16, p);
+            for (int j = 0; j < 8; ++j)
+                d.wR[j] = host_tw_entry(field, fpow(field, w16, j, p), p);
+        } else {
+            for (uint32_t j = 0; j < L / 2; ++j)
+                d.wR[j * 16 / L] = host_tw_entry(field, fpow(field, wL, j, p), p);
+        }
+        d.scale = host_tw_entry(field, ninv, p);
+        uint64_t col_limit;
+        if (i + 1 < K) {
+            d.mode = kModeCol;
+            d.tfast = 0;
+            d.logM = log_n - done;
+            d.logS = d.logM - d.logL;
+            d.h = (d.logM + 1) / 2;
+            const uint64_t wM = fpow(field, root_dir, n >> d.logM, p);
+            d.lo_off = add_table(1ull << d.h, wM, 1);
+            d.hi_off = add_table(1ull << (d.logM - d.h), fpow(field, wM, 1ull << d.h, p), i == 0 ? ninv : 1);
+            col_limit = 1ull << d.logS;
+        } else {
+            d.mode = kModeRow;
+            d.tfast = (K == 1) ? 1 : 0;
+            d.do_scale = (K == 1 && dir == STNTT_INVERSE) ? 1 : 0;
+            d.logN1 = K >= 2 ? logs[0] : 0;
+            d.logN2 = K == 3 ? logs[1] : 0;
+            col_limit = 1ull << 20;
+        }
+        shape_pass(d, field, n >> d.logL, col_limit);
+        pl.passes.push_back(d);
+        done += d.logL;
+    }
+    const size_t esz = 8;  // both fields: 8-byte twiddle entries
+    pl.table_bytes = off * esz;
+    cudaError_t e = cudaMalloc(&pl.d_tables, pl.table_bytes);
+    if (e != cudaSuccess) {
+        pl.d_tables = nullptr;
+        return cuda_fail(ctx, e, "cudaMalloc(twiddle tables)");
+    }
+    uint64_t o = 0;
+    for (const auto &r : reqs) {
+        e = launch_gen_powers(field, static_cast<char *>(pl.d_tables) + o * esz, r.count, r.base, r.scale, p,
+                              ctx->setup);
+        if (e != cudaSuccess)
+            return cuda_fail(ctx, e, "twiddle generation launch");
+        o += r.count;
+    }
+    e = cudaStreamSynchronize(ctx->setup);
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "twiddle generation");
+    return STNTT_OK;
+}
+
+int get_plan(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t p, uint64_t root, int dir, const Plan **out) {
+    const uint64_t rd = dir_root(field, root, p, dir);
+    PlanKey key{field, log_n, field == kFieldGL ? 0u : p, rd, dir};
+    std::lock_guard<std::mutex> g(ctx->mu);
+    auto it = ctx->plans.find(key);
+    if (it != ctx->plans.end()) {
+        *out = it->second.get();
+        return STNTT_OK;
+    }
+    auto pl = std::make_unique<Plan>();
+    ctx->mu.unlock();
+    int rc = build_plan(ctx, *pl, field, log_n, p, rd, dir);
+    ctx->mu.lock();
+    if (rc != STNTT_OK) {
+        if (pl->d_tables)
+            cudaFree(pl->d_tables);
+        return rc;
+    }
+    void *mine = pl->d_tables;
+    auto ins = ctx->plans.emplace(key, std::move(pl));
+    if (ins.second)
+        ctx->mem += ins.first->second->table_bytes;
+    else if (mine)
+        cudaFree(mine);  // another thread built the same plan first
+    *out = ins.first->second.get();
+    return STNTT_OK;
+}
+
+// Per-stream scratch of at least `bytes`.
+int get_workspace(stntt_ctx *ctx, cudaStream_t s, size_t bytes, void **ptr) {
+    std::lock_guard<std::mutex> g(ctx->mu);
+    DevBuf &b = ctx->workspaces[s];
+    if (b.bytes < bytes) {
+        if (b.ptr) {
+            cudaError_t e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess) {
+                ctx->err = std::string("workspace resize sync: ") + cudaGetErrorString(e);
+                return STNTT_ECUDA;
+            }
+            cudaFree(b.ptr);
+            ctx->mem -= b.bytes;
+            b.ptr = nullptr;
+            b.bytes = 0;
+        }
+        cudaError_t e = cudaMalloc(&b.ptr, bytes);
+        if (e != cudaSuccess) {
+            b.ptr = nullptr;
+            ctx->err = std::string("cudaMalloc(workspace): ") + cudaGetErrorString(e);
+            return e == cudaErrorMemoryAllocation ? STNTT_ENOMEM : STNTT_ECUDA;
+        }
+        b.bytes = bytes;
+        ctx->mem += bytes;
+    }
+    *ptr = b.ptr;
+    return STNTT_OK;
+}
+
+int check_u32_args(stntt_ctx *ctx, uint32_t log_n, uint32_t p, uint32_t root) {
+    if (log_n > 27)
+        return fail(ctx, STNTT_EUNSUPPORTED, "log_n must be <= 27 for the 32-bit field");
+    if (p < 2 || p >= (1u << 31))
+        return fail(ctx, STNTT_EINVAL, "p must be a prime in [2, 2^31)");
+    if (log_n > 0 && ((p - 1) % (1u << log_n)) != 0)
+        return fail(ctx, STNTT_EINVAL, "p - 1 must be divisible by n");
+    if (root == 0 || root >= p)
+        return fail(ctx, STNTT_EINVAL, "root must lie in [1, p)");
+    if (host_pow_mod(root, 1ull << log_n, p) != 1 || (log_n > 0 && host_pow_mod(root, 1ull << (log_n - 1), p) == 1))
+        return fail(ctx, STNTT_EINVAL, "root is not a primitive n-th root of unity mod p");
+    return STNTT_OK;
+}
+
+// Run a plan: first pass reads `in`, last pass writes `out`.
+int run_plan(stntt_ctx *ctx, const Plan &pl, const void *in, void *out, uint64_t batch, cudaStream_t s) {
+    const size_t esz = pl.field == kFieldGL ? 8 : 4;
+    const size_t bytes = (batch << pl.log_n) * esz;
+    if (pl.passes.empty()) {  // n == 1: the identity
+        if (in != out) {
+            cudaError_t e = cudaMemcpyAsync(out, in, bytes, cudaMemcpyDeviceToDevice, s);
+            if (e != cudaSuccess)
+                return cuda_fail(ctx, e, "cudaMemcpyAsync");
+        }
+        return STNTT_OK;
+    }
+    void *ws = nullptr;
+    if (pl.passes.size() > 1) {
+        int rc = get_workspace(ctx, s, bytes, &ws);
+        if (rc)
+            return rc;
+    }
+    const size_t K = pl.passes.size();
+    const void *src = in;
+    for (size_t i = 0; i < K; ++i) {
+        void *dst = (i + 1 == K) ? out : ws;
+        cudaError_t e = launch_tile(pl.field, pl.passes[i], pl.p, pl.d_tables, src, dst, batch, s);
+        if (e != cudaSuccess)
+            return cuda_fail(ctx, e, "tile kernel launch");
+        src = dst;
+    }
+    return STNTT_OK;
+}
+
+// int32 wrap-around twiddle table of the reference: t_0 = 1,
+// t_(i+1) = (t_i * root) % mod in 32-bit signed arithmetic (ntt_cpu.cpp:57-62).
+int get_stage_table(stntt_ctx *ctx, uint32_t log_n, uint32_t p, uint32_t root, int wrap, const void **out) {
+    std::lock_guard<std::mutex> g(ctx->mu);
+    auto key = std::make_tuple(log_n, p, root, wrap);
+    auto it = ctx->stage_tables.find(key);
+    if (it != ctx->stage_tables.end()) {
+        *out = it->second.ptr;
+        return STNTT_OK;
+    }
+    const uint64_t half = log_n ? (1ull << (log_n - 1)) : 0;
+    const size_t esz = wrap ? 4 : 8;
+    DevBuf b;
+    b.bytes = std::max<uint64_t>(half, 1) * esz;
+    cudaError_t e = cudaMalloc(&b.ptr, b.bytes);
+    if (e != cudaSuccess) {
+        ctx->err = std::string("cudaMalloc(stage table): ") + cudaGetErrorString(e);
+        return STNTT_ENOMEM;
+    }
+    if (wrap) {
+        std::vector<int32_t> t(std::max<uint64_t>(half, 1));
+        int32_t temp = 1;
+        for (uint64_t i = 0; i < half; ++i) {
+            t[i] = temp;
+            temp = (int32_t)((uint32_t)temp * (uint32_t)root) % (int32_t)p;
+        }
+        e = cudaMemcpy(b.ptr, t.data(), b.bytes, cudaMemcpyHostToDevice);
+    } else {
+        e = launch_gen_powers(kFieldU32, b.ptr, half, root, 1, p, ctx->setup);
+        if (e == cudaSuccess)
+            e = cudaStreamSynchronize(ctx->setup);
+    }
+    if (e != cudaSuccess) {
+        cudaFree(b.ptr);
+        ctx->err = std::string("stage table: ") + cudaGetErrorString(e);
+        return STNTT_ECUDA;
+    }
+    ctx->mem += b.bytes;
+    ctx->stage_tables[key] = b;
+    *out = b.ptr;
+    return STNTT_OK;
+}
+
+// Radix-2 Stockham stages one launch each (debug / reference-compatible path).
+int run_stages(stntt_ctx *ctx, uint32_t *d, uint32_t log_n, uint64_t batch, uint32_t p, uint32_t root,
+               uint32_t nsteps, int wrap, cudaStream_t s) {
+    if (nsteps == 0 || log_n == 0)
+        return STNTT_OK;
+    const void *tw = nullptr;
+    int rc = get_stage_table(ctx, log_n, p, root, wrap, &tw);
+    if (rc)
+        return rc;
+    const size_t bytes = (batch << log_n) * 4;
+    void *ws = nullptr;
+    rc = get_workspace(ctx, s, bytes, &ws);
+    if (rc)
+        return rc;
+    void *a = d, *b = ws;
+    for (uint32_t st = 0; st < nsteps; ++st) {
+        cudaError_t e = launch_stage_u32(a, b, tw, log_n, st, p, wrap, batch, s);
+        if (e != cudaSuccess)
+            return cuda_fail(ctx, e, "stage kernel launch");
+        std::swap(a, b);
+    }
+    if (a != d) {
+        cudaError_t e = cudaMemcpyAsync(d, a, bytes, cudaMemcpyDeviceToDevice, s);
+        if (e != cudaSuccess)
+            return cuda_fail(ctx, e, "cudaMemcpyAsync");
+    }
+    return STNTT_OK;
+}
+
+// Device staging buffer for the host-buffer entry points (caller holds host_mu).
+int host_stage(stntt_ctx *ctx, size_t bytes, void **ptr) {
+    DevBuf &b = ctx->host_stage;
+    if (b.bytes < bytes) {
+        if (b.ptr) {
+            cudaStreamSynchronize(ctx->host_stream);
+            cudaFree(b.ptr);
+            std::lock_guard<std::mutex> g(ctx->mu);
+            ctx->mem -= b.bytes;
+        }
+        b.ptr = nullptr;
+        b.bytes = 0;
+        cudaError_t e = cudaMalloc(&b.ptr, bytes);
+        if (e != cudaSuccess) {
+            b.ptr = nullptr;
+            return fail(ctx, STNTT_ENOMEM, std::string("cudaMalloc(host staging): ") + cudaGetErrorString(e));
+        }
+        b.bytes = bytes;
+        std::lock_guard<std::mutex> g(ctx->mu);
+        ctx->mem += bytes;
+    }
+    *ptr = b.ptr;
+    return STNTT_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+int stntt_version(void) { return STNTT_VERSION; }
+
+const char *stntt_status_string(int status) {
+    switch (status) {
+    case STNTT_OK: return "ok";
+    case STNTT_EINVAL: return "invalid argument";
+    case STNTT_ENOMEM: return "out of memory";
+    case STNTT_ECUDA: return "CUDA error";
+    case STNTT_ETIMEOUT: return "device wait timed out";
+    case STNTT_EUNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+    }
+}
+
+int stntt_init(stntt_ctx **out, int device) {
+    if (!out)
+        return STNTT_EINVAL;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count)
+        return STNTT_EINVAL;
+    auto ctx = new (std::nothrow) stntt_ctx();
+    if (!ctx)
+        return STNTT_ENOMEM;
+    ctx->device = device;
+    DeviceGuard g(device);
+    if (g.err != cudaSuccess || cudaStreamCreateWithFlags(&ctx->setup, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->host_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        if (ctx->setup)
+            cudaStreamDestroy(ctx->setup);
+        delete ctx;
+        return STNTT_ECUDA;
+    }
+    *out = ctx;
+    return STNTT_OK;
+}
+
+int stntt_destroy(stntt_ctx *ctx) {
+    if (!ctx)
+        return STNTT_EINVAL;
+    DeviceGuard g(ctx->device);
+    cudaDeviceSynchronize();
+    for (auto &kv : ctx->plans)
+        if (kv.second->d_tables)
+            cudaFree(kv.second->d_tables);
+    for (auto &kv : ctx->workspaces)
+        if (kv.second.ptr)
+            cudaFree(kv.second.ptr);
+    for (auto &kv : ctx->stage_tables)
+        if (kv.second.ptr)
+            cudaFree(kv.second.ptr);
+    if (ctx->host_stage.ptr)
+        cudaFree(ctx->host_stage.ptr);
+    if (ctx->setup)
+        cudaStreamDestroy(ctx->setup);
+    if (ctx->host_stream)
+        cudaStreamDestroy(ctx->host_stream);
+    delete ctx;
+    return STNTT_OK;
+}
+
+const char *stntt_last_error(const stntt_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int stntt_mem_usage(const stntt_ctx *ctx, size_t *bytes) {
+    if (!ctx || !bytes)
+        return STNTT_EINVAL;
+    *bytes = ctx->mem;
+    return STNTT_OK;
+}
+
+int stntt_find_params(uint64_t size, uint64_t min_mod, uint64_t *root, uint64_t *mod) {
+    if (!root || !mod || size == 0 || min_mod == 0)
+        return STNTT_EINVAL;
+    uint64_t k = std::max<uint64_t>((min_mod - 1 + size - 1) / size, 1);
+    uint64_t m = 0;
+    for (;; ++k) {
+        if (k > UINT64_MAX / size || k * size >= (1ull << 62))
+            return STNTT_EUNSUPPORTED;
+        if (is_prime_td(k * size + 1)) {
+            m = k * size + 1;
+            break;
+        }
+    }
+    const uint64_t tot = m - 1;
+    const std::vector<uint64_t> f = prime_factors(tot);
+    uint64_t g = 0;
+    for (uint64_t c = 1; c < m && !g; ++c) {
+        if (host_pow_mod(c, tot, m) != 1 % m)
+            continue;
+        bool ok = true;
+        for (uint64_t q : f)
+            if (host_pow_mod(c, tot / q, m) == 1) {
+                ok = false;
+                break;
+            }
+        if (ok)
+            g = c;
+    }
+    if (!g)
+        return STNTT_EUNSUPPORTED;
+    *mod = m;
+    *root = host_pow_mod(g, tot / size, m);
+    return STNTT_OK;
+}
+
+int stntt_params_u32(uint32_t log_n, uint32_t *p, uint32_t *root) {
+    if (!p || !root || log_n > 30)
+        return STNTT_EINVAL;
+    uint64_t r, m;
+    int rc = stntt_find_params(1ull << log_n, 11, &r, &m);
+    if (rc)
+        return rc;
+    if (m >= (1ull << 32))
+        return STNTT_EUNSUPPORTED;
+    *p = (uint32_t)m;
+    *root = (uint32_t)r;
+    return STNTT_OK;
+}
+
+int stntt_gl64_root(uint32_t log_n, uint64_t *root) {
+    if (!root || log_n > 32)
+        return STNTT_EINVAL;
+    *root = host_gl_pow(7, (GL_P - 1) >> log_n);
+    return STNTT_OK;
+}
+
+int stntt_prepare(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t p, uint32_t root, int dir) {
+    if (!ctx || (dir != STNTT_FORWARD && dir != STNTT_INVERSE))
+        return fail(ctx, STNTT_EINVAL, "bad context or direction");
+    DeviceGuard g(ctx->device);
+    const Plan *pl;
+    if (field == STNTT_FIELD_GL64) {
+        if (log_n > 32)
+            return fail(ctx, STNTT_EUNSUPPORTED, "log_n must be <= 32 for Goldilocks");
+        uint64_t r;
+        stntt_gl64_root(log_n, &r);
+        return get_plan(ctx, kFieldGL, log_n, 0, r, dir, &pl);
+    }
+    if (field != STNTT_FIELD_U32)
+        return fail(ctx, STNTT_EINVAL, "unknown field");
+    int rc = check_u32_args(ctx, log_n, p, root);
+    if (rc)
+        return rc;
+    return get_plan(ctx, kFieldU32, log_n, p, root, dir, &pl);
+}
+
+int stntt_plan_info(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t p, uint32_t root, int dir,
+                    uint32_t *passes, uint32_t *pass_logs) {
+    if (!ctx || !passes)
+        return STNTT_EINVAL;
+    int rc = stntt_prepare(ctx, field, log_n, p, root, dir);
+    if (rc)
+        return rc;
+    const Plan *pl;
+    uint64_t r = root;
+    if (field == STNTT_FIELD_GL64)
+        stntt_gl64_root(log_n, &r);
+    rc = get_plan(ctx, field == STNTT_FIELD_GL64 ? kFieldGL : kFieldU32, log_n, field == STNTT_FIELD_GL64 ? 0 : p,
+                  r, dir, &pl);
+    if (rc)
+        return rc;
+    *passes = (uint32_t)pl->passes.size();
+    if (pass_logs)
+        for (size_t i = 0; i < pl->passes.size() && i < 4; ++i)
+            pass_logs[i] = pl->passes[i].logL;
+    return STNTT_OK;
+}
+
+int stntt_ntt_u32_oop(stntt_ctx *ctx, const uint32_t *d_in, uint32_t *d_out, uint32_t log_n, uint32_t batch,
+                      uint32_t p, uint32_t root, int dir, stntt_stream stream) {
+    if (!ctx)
+        return STNTT_EINVAL;
+    if ((!d_in || !d_out) && batch)
+        return fail(ctx, STNTT_EINVAL, "null data pointer");
+    if (dir != STNTT_FORWARD && dir != STNTT_INVERSE)
+        return fail(ctx, STNTT_EINVAL, "dir must be STNTT_FORWARD or STNTT_INVERSE");
+    int rc = check_u32_args(ctx, log_n, p, root);
+    if (rc)
+        return rc;
+    if (batch == 0)
+        return STNTT_OK;
+    DeviceGuard g(ctx->device);
+    const Plan *pl;
+    rc = get_plan(ctx, kFieldU32, log_n, p, root, dir, &pl);
+    if (rc)
+        return rc;
+    return run_plan(ctx, *pl, d_in, d_out, batch, (cudaStream_t)stream);
+}
+
+int stntt_ntt_u32(stntt_ctx *ctx, uint32_t *d_data, uint32_t log_n, uint32_t batch, uint32_t p, uint32_t root,
+                  int dir, uint32_t flags, stntt_stream stream) {
+    if (!ctx)
+        return STNTT_EINVAL;
+    if (flags & ~STNTT_FLAG_REF_WRAP)
+        return fail(ctx, STNTT_EINVAL, "unknown flags");
+    if (flags & STNTT_FLAG_REF_WRAP) {
+        if (dir != STNTT_FORWARD)
+            return fail(ctx, STNTT_EINVAL, "STNTT_FLAG_REF_WRAP supports the forward transform only");
+        return stntt_ntt_u32_steps(ctx, d_data, log_n, batch, p, root, log_n, flags, stream);
+    }
+    return stntt_ntt_u32_oop(ctx, d_data, d_data, log_n, batch, p, root, dir, stream);
+}
+
+int stntt_ntt_u32_steps(stntt_ctx *ctx, uint32_t *d_data, uint32_t log_n, uint32_t batch, uint32_t p,
+                        uint32_t root, uint32_t nsteps, uint32_t flags, stntt_stream stream) {
+    if (!ctx)
+        return STNTT_EINVAL;
+    if (!d_data && batch)
+        return fail(ctx, STNTT_EINVAL, "null data pointer");
+    if (flags & ~STNTT_FLAG_REF_WRAP)
+        return fail(ctx, STNTT_EINVAL, "unknown flags");
+    if (nsteps > log_n)
+        return fail(ctx, STNTT_EINVAL, "nsteps must be <= log_n");
+    const int wrap = (flags & STNTT_FLAG_REF_WRAP) ? 1 : 0;
+    if (wrap) {  // the reference accepts any int modulus / root; only the size limits apply
+        if (log_n > 30 || p < 2 || p >= (1u << 31))
+            return fail(ctx, STNTT_EINVAL, "REF_WRAP needs log_n <= 30 and 2 <= p < 2^31");
+    } else {
+        int rc = check_u32_args(ctx, log_n, p, root);
+        if (rc)
+            return rc;
+    }
+    if (batch == 0)
+        return STNTT_OK;
+    DeviceGuard g(ctx->device);
+    return run_stages(ctx, d_data, log_n, batch, p, root, nsteps, wrap, (cudaStream_t)stream);
+}
+
+int stntt_ntt_gl64_oop(stntt_ctx *ctx, const uint64_t *d_in, uint64_t *d_out, uint32_t log_n, uint32_t batch,
+                       int dir, stntt_stream stream) {
+    if (!ctx)
+        return STNTT_EINVAL;
+    if ((!d_in || !d_out) && batch)
+        return fail(ctx, STNTT_EINVAL, "null data pointer");
+    if (dir != STNTT_FORWARD && dir != STNTT_INVERSE)
+        return fail(ctx, STNTT_EINVAL, "dir must be STNTT_FORWARD or STNTT_INVERSE");
+    if (log_n > 32)
+        return fail(ctx, STNTT_EUNSUPPORTED, "log_n must be <= 32 for Goldilocks");
+    if (batch == 0)
+        return STNTT_OK;
+    DeviceGuard g(ctx->device);
+    uint64_t r;
+    stntt_gl64_root(log_n, &r);
+    const Plan *pl;
+    int rc = get_plan(ctx, kFieldGL, log_n, 0, r, dir, &pl);
+    if (rc)
+        return rc;
+    return run_plan(ctx, *pl, d_in, d_out, batch, (cudaStream_t)stream);
+}
+
+int stntt_ntt_gl64(stntt_ctx *ctx, uint64_t *d_data, uint32_t log_n, uint32_t batch, int dir, stntt_stream stream) {
+    return stntt_ntt_gl64_oop(ctx, d_data, d_data, log_n, batch, dir, stream);
+}
+
+int stntt_ntt_stockham_host(stntt_ctx *ctx, int32_t *vec, int32_t size, int32_t root, int32_t mod, int32_t batches,
+                            int32_t nsteps, uint32_t flags) {
+    if (!ctx)
+        return STNTT_EINVAL;
+    if (size <= 0 || (size & (size - 1)))
+        return fail(ctx, STNTT_EINVAL, "size (" + std::to_string(size) + ") must be a power of 2");
+    if (!vec || batches < 0)
+        return fail(ctx, STNTT_EINVAL, "null vector or negative batch count");
+    if (mod < 2)
+        return fail(ctx, STNTT_EINVAL, "mod must be >= 2");
+    if (batches == 0)
+        return STNTT_OK;
+    const uint32_t log_n = ilog2((uint64_t)size);
+    if (nsteps > (int32_t)log_n)
+        return fail(ctx, STNTT_EINVAL, "nsteps must be <= log2(size)");
+    const bool wrap = (flags & STNTT_FLAG_REF_WRAP) != 0;
+    const size_t count = (size_t)size * (size_t)batches;
+    std::vector<int32_t> staged;
+    const int32_t *src = vec;
+    if (!wrap) {  // the exact field transform takes canonical residues
+        staged.assign(vec, vec + count);
+        for (auto &v : staged) {
+            int32_t r = v % mod;
+            v = r >= 0 ? r : r + mod;
+        }
+        src = staged.data();
+    }
+    DeviceGuard g(ctx->device);
+    std::lock_guard<std::mutex> hl(ctx->host_mu);
+    void *dv = nullptr;
+    int rc = host_stage(ctx, count * 4, &dv);
+    if (rc)
+        return rc;
+    uint32_t *d = static_cast<uint32_t *>(dv);
+    cudaStream_t s = ctx->host_stream;
+    cudaError_t e = cudaMemcpyAsync(d, src, count * 4, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "host copy in");
+    if (nsteps >= 0 && (uint32_t)nsteps < log_n)
+        rc = stntt_ntt_u32_steps(ctx, d, log_n, (uint32_t)batches, (uint32_t)mod, (uint32_t)root, (uint32_t)nsteps,
+                                 flags, s);
+    else
+        rc = stntt_ntt_u32(ctx, d, log_n, (uint32_t)batches, (uint32_t)mod, (uint32_t)root, STNTT_FORWARD, flags, s);
+    if (rc) {
+        cudaStreamSynchronize(s);
+        return rc;
+    }
+    e = cudaMemcpyAsync(vec, d, count * 4, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "host copy out");
+    return STNTT_OK;
+}
+
+int stntt_ntt_gl64_host(stntt_ctx *ctx, uint64_t *vec, uint32_t log_n, uint32_t batch, int dir) {
+    if (!ctx)
+        return STNTT_EINVAL;
+    if (!vec && batch)
+        return fail(ctx, STNTT_EINVAL, "null vector");
+    if (log_n > 32)
+        return fail(ctx, STNTT_EUNSUPPORTED, "log_n must be <= 32 for Goldilocks");
+    if (batch == 0)
+        return STNTT_OK;
+    const size_t count = (size_t)batch << log_n;
+    DeviceGuard g(ctx->device);
+    std::lock_guard<std::mutex> hl(ctx->host_mu);
+    void *dv = nullptr;
+    int rc = host_stage(ctx, count * 8, &dv);
+    if (rc)
+        return rc;
+    cudaStream_t s = ctx->host_stream;
+    cudaError_t e = cudaMemcpyAsync(dv, vec, count * 8, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "host copy in");
+    rc = stntt_ntt_gl64(ctx, static_cast<uint64_t *>(dv), log_n, batch, dir, s);
+    if (rc) {
+        cudaStreamSynchronize(s);
+        return rc;
+    }
+    e = cudaMemcpyAsync(vec, dv, count * 8, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "host copy out");
+    return STNTT_OK;
+}
+
+int stntt_ntt_batch_per_call(stntt_ctx *ctx, const stntt_job *jobs, size_t njobs, stntt_stream stream) {
+    if (!ctx || (!jobs && njobs))
+        return STNTT_EINVAL;
+    for (size_t i = 0; i < njobs; ++i) {
+        const stntt_job &j = jobs[i];
+        int rc;
+        if (j.field == STNTT_FIELD_GL64)
+            rc = stntt_ntt_gl64(ctx, static_cast<uint64_t *>(j.data), j.log_n, 1, (int)j.dir, stream);
+        else if (j.field == STNTT_FIELD_U32)
+            rc = stntt_ntt_u32(ctx, static_cast<uint32_t *>(j.data), j.log_n, 1, j.p, j.root, (int)j.dir, 0, stream);
+        else
+            rc = fail(ctx, STNTT_EINVAL, "unknown field in job");
+        if (rc)
+            return rc;
+    }
+    return STNTT_OK;
+}
+
+int stntt_ntt_batch(stntt_ctx *ctx, const stntt_job *jobs, size_t njobs, stntt_stream stream) {
+    return stntt_ntt_batch_per_call(ctx, jobs, njobs, stream);
+}
+
+int stntt_pointwise_mul_u32(const uint32_t *d_a, const uint32_t *d_b, uint32_t *d_out, size_t count, uint32_t p,
+                            stntt_stream stream) {
+    if ((!d_a || !d_b || !d_out) && count)
+        return STNTT_EINVAL;
+    if (p < 2 || p >= (1u << 31))
+        return STNTT_EINVAL;
+    if (!count)
+        return STNTT_OK;
+    return launch_pointwise(kFieldU32, d_a, d_b, d_out, count, p, (cudaStream_t)stream) == cudaSuccess ? STNTT_OK
+                                                                                                      : STNTT_ECUDA;
+}
+
+int stntt_pointwise_mul_gl64(const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_out, size_t count,
+                             stntt_stream stream) {
+    if ((!d_a || !d_b || !d_out) && count)
+        return STNTT_EINVAL;
+    if (!count)
+        return STNTT_OK;
+    return launch_pointwise(kFieldGL, d_a, d_b, d_out, count, 0, (cudaStream_t)stream) == cudaSuccess ? STNTT_OK
+                                                                                                     : STNTT_ECUDA;
+}
+
+static int polymul_impl(stntt_ctx *ctx, int field, const void *a, const void *b, void *out, uint32_t log_n,
+                        uint32_t p, uint64_t root, cudaStream_t s) {
+    const size_t esz = field == kFieldGL ? 8 : 4;
+    const size_t bytes = ((size_t)1 << log_n) * esz;
+    const Plan *fwd, *inv;
+    int rc = get_plan(ctx, field, log_n, p, root, STNTT_FORWARD, &fwd);
+    if (!rc)
+        rc = get_plan(ctx, field, log_n, p, root, STNTT_INVERSE, &inv);
+    if (rc)
+        return rc;
+    // workspace: [pass scratch n][second operand n]
+    void *ws = nullptr;
+    rc = get_workspace(ctx, s, 2 * bytes, &ws);
+    if (rc)
+        return rc;
+    void *tb = static_cast<char *>(ws) + bytes;
+    // b first: `out` may alias `b`
+    if ((rc = run_plan(ctx, *fwd, b, tb, 1, s)))
+        return rc;
+    if ((rc = run_plan(ctx, *fwd, a, out, 1, s)))
+        return rc;
+    cudaError_t e = launch_pointwise(field, out, tb, out, (size_t)1 << log_n, p, s);
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "pointwise launch");
+    return run_plan(ctx, *inv, out, out, 1, s);
+}
+
+int stntt_polymul_u32(stntt_ctx *ctx, const uint32_t *d_a, const uint32_t *d_b, uint32_t *d_out, uint32_t log_n,
+                      uint32_t p, uint32_t root, stntt_stream stream) {
+    if (!ctx)
+        return STNTT_EINVAL;
+    if (!d_a || !d_b || !d_out)
+        return fail(ctx, STNTT_EINVAL, "null pointer");
+    int rc = check_u32_args(ctx, log_n, p, root);
+    if (rc)
+        return rc;
+    DeviceGuard g(ctx->device);
+    return polymul_impl(ctx, kFieldU32, d_a, d_b, d_out, log_n, p, root, (cudaStream_t)stream);
+}
+
+int stntt_polymul_gl64(stntt_ctx *ctx, const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_out, uint32_t log_n,
+                       stntt_stream stream) {
+    if (!ctx)
+        return STNTT_EINVAL;
+    if (!d_a || !d_b || !d_out)
+        return fail(ctx, STNTT_EINVAL, "null pointer");
+    if (log_n > 32)
+        return fail(ctx, STNTT_EUNSUPPORTED, "log_n must be <= 32 for Goldilocks");
+    DeviceGuard g(ctx->device);
+    uint64_t r;
+    stntt_gl64_root(log_n, &r);
+    return polymul_impl(ctx, kFieldGL, d_a, d_b, d_out, log_n, 0, r, (cudaStream_t)stream);
+}
+
+int stntt_fill_uniform_u32(uint32_t *d_out, size_t count, uint64_t seed, uint32_t p, stntt_stream stream) {
+    if ((!d_out && count) || p < 2)
+        return STNTT_EINVAL;
+    if (!count)
+        return STNTT_OK;
+    return launch_fill_uniform(kFieldU32, d_out, count, seed, p, (cudaStream_t)stream) == cudaSuccess ? STNTT_OK
+                                                                                                      : STNTT_ECUDA;
+}
+
+int stntt_fill_uniform_gl64(uint64_t *d_out, size_t count, uint64_t seed, stntt_stream stream) {
+    if (!d_out && count)
+        return STNTT_EINVAL;
+    if (!count)
+        return STNTT_OK;
+    return launch_fill_uniform(kFieldGL, d_out, count, seed, 0, (cudaStream_t)stream) == cudaSuccess ? STNTT_OK
+                                                                                                     : STNTT_ECUDA;
+}
+
+}  // extern "C"

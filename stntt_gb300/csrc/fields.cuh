@@ -1,0 +1,132 @@
+// fields.cuh -- modular arithmetic for the two NTT fields (device side).
+//
+// FieldU32: a runtime prime p < 2^31 (the reference's per-size prime from
+//   findParams, src/ntt/ntt_util.cpp:10-49). Replaces the reference's
+//   butterfly with three runtime '%' (src/cuda/ntt/arithmetic.cuh:17-24,
+//   src/cuda/math.cuh:10-16). Twiddles are Shoup pairs (w, floor(w*2^32/p)),
+//   so a twiddle product costs one mul.hi and two mul.lo.
+// FieldGL: Goldilocks p = 2^64 - 2^32 + 1. The reference has add/sub only
+//   (src/cuda/ntt/implementations/goldilocks/arithmetic.cuh:19-30; mul and
+//   butterfly are empty at :32-35). Products are 64x64->128 mad.lo/mad.hi
+//   chains reduced with 2^64 = 2^32 - 1 and 2^96 = -1 (mod p).
+// All values are kept canonical (< p).
+#pragma once
+#include <cstdint>
+
+namespace stntt {
+
+struct FieldU32 {
+    using T = uint32_t;
+    using TW = uint2;  // {w, floor(w * 2^32 / p)}
+    uint32_t p;
+
+    __device__ __forceinline__ T add(T a, T b) const {
+        uint32_t s = a + b;
+        return min(s, s - p);
+    }
+    __device__ __forceinline__ T sub(T a, T b) const {
+        uint32_t d = a - b + p;
+        return min(d, d - p);
+    }
+    // Shoup: q = floor(a * w' / 2^32); a*w - q*p lies in [0, 2p).
+    __device__ __forceinline__ T mul_tw(T a, TW w) const {
+        uint32_t q = __umulhi(a, w.y);
+        uint32_t r = a * w.x - q * p;
+        return min(r, r - p);
+    }
+    // General product of two residues (pointwise products).
+    __device__ __forceinline__ T mul(T a, T b) const { return (uint32_t)(((uint64_t)a * b) % p); }
+    __device__ __forceinline__ static T tw_value(TW w) { return w.x; }
+};
+
+struct FieldGL {
+    using T = uint64_t;
+    using TW = uint64_t;
+    static constexpr uint64_t P = 0xFFFFFFFF00000001ull;
+    uint32_t p;  // unused; keeps the two field types interchangeable
+
+    __device__ __forceinline__ T add(T a, T b) const {
+        // s = a + b; if (carry or s >= p) s = s + (2^32 - 1) mod 2^64.
+        uint32_t s0, s1;
+        asm("{\n\t"
+            ".reg .u32 c, d, x0, x1;\n\t"
+            ".reg .pred q;\n\t"
+            "add.cc.u32 %0, %2, %4;\n\t"
+            "addc.cc.u32 %1, %3, %5;\n\t"
+            "addc.u32 c, 0, 0;\n\t"
+            "add.cc.u32 x0, %0, 0xffffffff;\n\t"
+            "addc.cc.u32 x1, %1, 0;\n\t"
+            "addc.u32 d, c, 0;\n\t"
+            "setp.ne.u32 q, d, 0;\n\t"
+            "selp.u32 %0, x0, %0, q;\n\t"
+            "selp.u32 %1, x1, %1, q;\n\t"
+            "}"
+            : "=&r"(s0), "=&r"(s1)
+            : "r"((uint32_t)a), "r"((uint32_t)(a >> 32)), "r"((uint32_t)b), "r"((uint32_t)(b >> 32)));
+        return ((uint64_t)s1 << 32) | s0;
+    }
+
+    __device__ __forceinline__ T sub(T a, T b) const {
+        // d = a - b; on borrow d += p, i.e. d -= 2^32 - 1 (mod 2^64).
+        uint32_t d0, d1;
+        asm("{\n\t"
+            ".reg .u32 m;\n\t"
+            "sub.cc.u32 %0, %2, %4;\n\t"
+            "subc.cc.u32 %1, %3, %5;\n\t"
+            "subc.u32 m, 0, 0;\n\t"
+            "sub.cc.u32 %0, %0, m;\n\t"
+            "subc.u32 %1, %1, 0;\n\t"
+            "}"
+            : "=&r"(d0), "=&r"(d1)
+            : "r"((uint32_t)a), "r"((uint32_t)(a >> 32)), "r"((uint32_t)b), "r"((uint32_t)(b >> 32)));
+        return ((uint64_t)d1 << 32) | d0;
+    }
+
+    __device__ __forceinline__ T mul(T a, T b) const {
+        uint32_t r0, r1;
+        asm("{\n\t"
+            ".reg .u32 r2, r3, t0, t1, m, u0, u1, c, x0, x1, d;\n\t"
+            ".reg .pred q;\n\t"
+            // 128-bit product (r3:r2:r1:r0) = a * b
+            "mul.lo.u32 %0, %2, %4;\n\t"
+            "mul.hi.u32 %1, %2, %4;\n\t"
+            "mad.lo.cc.u32 %1, %2, %5, %1;\n\t"
+            "madc.hi.u32 r2, %2, %5, 0;\n\t"
+            "mad.lo.cc.u32 %1, %3, %4, %1;\n\t"
+            "madc.hi.cc.u32 r2, %3, %4, r2;\n\t"
+            "madc.hi.u32 r3, %3, %5, 0;\n\t"
+            "mad.lo.cc.u32 r2, %3, %5, r2;\n\t"
+            "addc.u32 r3, r3, 0;\n\t"
+            // t = (r1:r0) - r3; on borrow t -= 2^32 - 1
+            "sub.cc.u32 t0, %0, r3;\n\t"
+            "subc.cc.u32 t1, %1, 0;\n\t"
+            "subc.u32 m, 0, 0;\n\t"
+            "sub.cc.u32 t0, t0, m;\n\t"
+            "subc.u32 t1, t1, 0;\n\t"
+            // u = r2 * (2^32 - 1) = (r2 << 32) - r2
+            "sub.cc.u32 u0, 0, r2;\n\t"
+            "subc.u32 u1, r2, 0;\n\t"
+            // s = t + u; on carry s += 2^32 - 1 (cannot carry again)
+            "add.cc.u32 t0, t0, u0;\n\t"
+            "addc.cc.u32 t1, t1, u1;\n\t"
+            "addc.u32 c, 0, 0;\n\t"
+            "neg.s32 c, c;\n\t"
+            "add.cc.u32 t0, t0, c;\n\t"
+            "addc.u32 t1, t1, 0;\n\t"
+            // canonical: if s >= p then s -= p (s + 2^32 - 1 carries out)
+            "add.cc.u32 x0, t0, 0xffffffff;\n\t"
+            "addc.cc.u32 x1, t1, 0;\n\t"
+            "addc.u32 d, 0, 0;\n\t"
+            "setp.ne.u32 q, d, 0;\n\t"
+            "selp.u32 %0, x0, t0, q;\n\t"
+            "selp.u32 %1, x1, t1, q;\n\t"
+            "}"
+            : "=&r"(r0), "=&r"(r1)
+            : "r"((uint32_t)a), "r"((uint32_t)(a >> 32)), "r"((uint32_t)b), "r"((uint32_t)(b >> 32)));
+        return ((uint64_t)r1 << 32) | r0;
+    }
+    __device__ __forceinline__ T mul_tw(T a, TW w) const { return mul(a, w); }
+    __device__ __forceinline__ static T tw_value(TW w) { return w; }
+};
+
+}  // namespace stntt

@@ -1,0 +1,50 @@
+// internal.h -- interface between the host planner (api.cu) and the per-field
+// kernel translation units (kernels_u32.cu, kernels_gl64.cu). Not installed.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+namespace stntt {
+
+enum : int { kFieldU32 = 0, kFieldGL = 1 };
+enum : uint32_t { kModeCol = 0, kModeRow = 1 };  // tile pass kinds (tile.cuh)
+
+// One HBM pass of a transform plan (see tile.cuh for the meaning of the fields).
+struct PassDesc {
+    uint32_t logL = 0, logC = 0, E = 16, mode = 1, do_scale = 0, tfast = 1, h = 0;
+    uint32_t logN = 0, logM = 0, logS = 0, logN1 = 0, logN2 = 0;
+    uint32_t cs = 0;          // shared-memory column stride, elements
+    uint32_t threads = 0;     // threads per CTA
+    size_t smem_bytes = 0;
+    uint64_t tw_off = 0, lo_off = 0, hi_off = 0;  // table offsets, in table entries
+    uint64_t wR[8] = {};      // raw twiddle entries (u32: {w, w'} packed little-endian)
+    uint64_t scale = 0;       // raw twiddle entry
+};
+
+// ---- launchers (return the CUDA error of the launch) ----------------------
+cudaError_t launch_tile(int field, const PassDesc &d, uint32_t p, const void *tables, const void *in, void *out,
+                        uint64_t batch, cudaStream_t s);
+// out[i] = scale * base^i, i < count, as twiddle entries (u32: Shoup pairs).
+cudaError_t launch_gen_powers(int field, void *out, uint64_t count, uint64_t base, uint64_t scale, uint32_t p,
+                              cudaStream_t s);
+cudaError_t launch_pointwise(int field, const void *a, const void *b, void *out, size_t count, uint32_t p,
+                             cudaStream_t s);
+cudaError_t launch_fill_uniform(int field, void *out, size_t count, uint64_t seed, uint32_t p, cudaStream_t s);
+// One radix-2 Stockham DIF stage (src/ntt/ntt_cpu.cpp:66-79) over `batch`
+// transforms. wrap != 0: the reference's int32 arithmetic with its wrapped
+// twiddle table (int32 entries); else exact with a Shoup-pair table.
+cudaError_t launch_stage_u32(const void *in, void *out, const void *tw, uint32_t log_n, uint32_t stage, uint32_t p,
+                             int wrap, uint64_t batch, cudaStream_t s);
+cudaError_t launch_copy_scale(int field, const void *in, void *out, size_t count, uint64_t scale_tw, uint32_t p,
+                              cudaStream_t s);
+
+// Host modular helpers
+uint64_t host_pow_mod(uint64_t b, uint64_t e, uint64_t m);
+uint64_t host_gl_mul(uint64_t a, uint64_t b);
+uint64_t host_gl_pow(uint64_t b, uint64_t e);
+// Twiddle entry for a value (u32: {w, floor(w * 2^32 / p)} packed; gl: w)
+uint64_t host_tw_entry(int field, uint64_t w, uint32_t p);
+
+}  // namespace stntt

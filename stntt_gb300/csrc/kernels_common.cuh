@@ -1,0 +1,139 @@
+// kernels_common.cuh -- field-generic kernels and launchers, instantiated once
+// per field by kernels_u32.cu and kernels_gl64.cu.
+#pragma once
+#include <cstring>
+
+#include "internal.h"
+#include "tile.cuh"
+
+namespace stntt {
+
+template <class F>
+__device__ __forceinline__ typename F::TW to_tw(uint64_t raw) {
+    typename F::TW w;
+    memcpy(&w, &raw, sizeof(w));
+    return w;
+}
+
+template <class F, int E, int TAIL>
+cudaError_t launch_tile_e(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks, cudaStream_t s) {
+    auto kern = tile_kernel<F, E, TAIL>;
+    static bool attr_set[64] = {};  // per device: the opt-in shared-memory size of this kernel
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+        return e;
+    if (dev < 0 || dev >= 64)
+        return cudaErrorInvalidDevice;
+    if (!attr_set[dev]) {
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        if (e != cudaSuccess)
+            return e;
+        attr_set[dev] = true;
+    }
+    if (d.smem_bytes > 200 * 1024)
+        return cudaErrorInvalidConfiguration;
+    kern<<<(unsigned)blocks, d.threads, d.smem_bytes, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <class F>
+cudaError_t launch_tile_t(const PassDesc &d, uint32_t p, const void *tables, const void *in, void *out,
+                          uint64_t batch, cudaStream_t s) {
+    using T = typename F::T;
+    using TW = typename F::TW;
+    TileArgs<F> a;
+    const TW *tab = static_cast<const TW *>(tables);
+    a.in = static_cast<const T *>(in);
+    a.out = static_cast<T *>(out);
+    a.twL = tab + d.tw_off;
+    a.tw4_lo = tab + d.lo_off;
+    a.tw4_hi = tab + d.hi_off;
+    for (int j = 0; j < 8; ++j)
+        std::memcpy(&a.wR[j], &d.wR[j], sizeof(TW));
+    std::memcpy(&a.scale, &d.scale, sizeof(TW));
+    a.p = p;
+    a.logL = d.logL;
+    a.logC = d.logC;
+    a.mode = d.mode;
+    a.do_scale = d.do_scale;
+    a.tfast = d.tfast;
+    a.h = d.h;
+    a.logN = d.logN;
+    a.logM = d.logM;
+    a.logS = d.logS;
+    a.logN1 = d.logN1;
+    a.logN2 = d.logN2;
+    a.cs = d.cs;
+    const uint64_t rows = batch << (d.logN - d.logL);
+    a.total = rows;
+    const uint64_t blocks = (rows + (1ull << d.logC) - 1) >> d.logC;
+    if (blocks == 0)
+        return cudaSuccess;
+    if (blocks > 0x7fffffffull)
+        return cudaErrorInvalidConfiguration;
+    const uint32_t tail = d.logL & 3;
+    switch (d.E) {
+    case 2: return launch_tile_e<F, 2, 1>(d, a, blocks, s);
+    case 4: return launch_tile_e<F, 4, 2>(d, a, blocks, s);
+    case 8: return launch_tile_e<F, 8, 3>(d, a, blocks, s);
+    case 16:
+        switch (tail) {
+        case 0: return launch_tile_e<F, 16, 0>(d, a, blocks, s);
+        case 1: return launch_tile_e<F, 16, 1>(d, a, blocks, s);
+        case 2: return launch_tile_e<F, 16, 2>(d, a, blocks, s);
+        default: return launch_tile_e<F, 16, 3>(d, a, blocks, s);
+        }
+    case 32:
+        switch (tail) {
+        case 0: return launch_tile_e<F, 32, 0>(d, a, blocks, s);
+        case 1: return launch_tile_e<F, 32, 1>(d, a, blocks, s);
+        case 2: return launch_tile_e<F, 32, 2>(d, a, blocks, s);
+        default: return launch_tile_e<F, 32, 3>(d, a, blocks, s);
+        }
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+// out[i] = scale * base^i as twiddle entries
+template <class F>
+__global__ void gen_powers_kernel(typename F::TW *out, uint64_t count, uint64_t base, uint64_t scale, uint32_t p);
+
+template <class F>
+__global__ void pointwise_kernel(const typename F::T *a, const typename F::T *b, typename F::T *out, size_t count,
+                                 uint32_t p) {
+    F f;
+    f.p = p;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride)
+        out[i] = f.mul(a[i], b[i]);
+}
+
+template <class F>
+__global__ void copy_scale_kernel(const typename F::T *in, typename F::T *out, size_t count, uint64_t scale_raw,
+                                  uint32_t p) {
+    F f;
+    f.p = p;
+    const typename F::TW w = to_tw<F>(scale_raw);
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride)
+        out[i] = f.mul_tw(in[i], w);
+}
+
+__device__ __forceinline__ uint64_t sm64_mix(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+__device__ __forceinline__ uint64_t sm64_draw(uint64_t seed, uint64_t i, uint64_t attempt) {
+    return sm64_mix(seed + 0x9E3779B97F4A7C15ull * (i + (attempt << 40) + 1ull));
+}
+
+inline unsigned grid_for(size_t count, unsigned threads) {
+    size_t b = (count + threads - 1) / threads;
+    if (b > 152u * 32u)
+        b = 152u * 32u;
+    return (unsigned)(b ? b : 1);
+}
+
+}  // namespace stntt

@@ -1,0 +1,67 @@
+// kernels_gl64.cu -- kernels over Goldilocks, p = 2^64 - 2^32 + 1.
+#include "kernels_common.cuh"
+
+namespace stntt {
+
+template <>
+__global__ void gen_powers_kernel<FieldGL>(uint64_t *out, uint64_t count, uint64_t base, uint64_t scale,
+                                           uint32_t) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count)
+        return;
+    FieldGL f;
+    uint64_t r = scale, b = base;
+    for (uint64_t e = i; e; e >>= 1) {
+        if (e & 1)
+            r = f.mul(r, b);
+        b = f.mul(b, b);
+    }
+    out[i] = r;
+}
+
+__global__ void fill_uniform_gl64_kernel(uint64_t *out, size_t count, uint64_t seed) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+        uint64_t x = 0;
+        for (uint64_t a = 0;; ++a) {
+            x = sm64_draw(seed, i, a);
+            if (x < FieldGL::P)
+                break;
+        }
+        out[i] = x;
+    }
+}
+
+cudaError_t launch_tile_gl64(const PassDesc &d, uint32_t p, const void *tables, const void *in, void *out,
+                             uint64_t batch, cudaStream_t s) {
+    return launch_tile_t<FieldGL>(d, p, tables, in, out, batch, s);
+}
+
+cudaError_t gen_powers_gl64(void *out, uint64_t count, uint64_t base, uint64_t scale, cudaStream_t s) {
+    const unsigned threads = 256;
+    const uint64_t blocks = (count + threads - 1) / threads;
+    if (!blocks)
+        return cudaSuccess;
+    gen_powers_kernel<FieldGL><<<(unsigned)blocks, threads, 0, s>>>(static_cast<uint64_t *>(out), count, base, scale,
+                                                                    0);
+    return cudaGetLastError();
+}
+
+cudaError_t pointwise_gl64(const void *a, const void *b, void *out, size_t count, cudaStream_t s) {
+    pointwise_kernel<FieldGL><<<grid_for(count, 256), 256, 0, s>>>(
+        static_cast<const uint64_t *>(a), static_cast<const uint64_t *>(b), static_cast<uint64_t *>(out), count, 0);
+    return cudaGetLastError();
+}
+
+cudaError_t fill_uniform_gl64(void *out, size_t count, uint64_t seed, cudaStream_t s) {
+    fill_uniform_gl64_kernel<<<grid_for(count, 256), 256, 0, s>>>(static_cast<uint64_t *>(out), count, seed);
+    return cudaGetLastError();
+}
+
+cudaError_t copy_scale_gl64(const void *in, void *out, size_t count, uint64_t scale_tw, cudaStream_t s) {
+    copy_scale_kernel<FieldGL><<<grid_for(count, 256), 256, 0, s>>>(static_cast<const uint64_t *>(in),
+                                                                    static_cast<uint64_t *>(out), count, scale_tw, 0);
+    return cudaGetLastError();
+}
+
+}  // namespace stntt

@@ -1,0 +1,117 @@
+// kernels_u32.cu -- kernels over the reference's per-size 32-bit prime field.
+#include "kernels_common.cuh"
+
+namespace stntt {
+
+template <>
+__global__ void gen_powers_kernel<FieldU32>(uint2 *out, uint64_t count, uint64_t base, uint64_t scale, uint32_t p) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count)
+        return;
+    uint64_t r = scale % p, b = base % p;
+    for (uint64_t e = i; e; e >>= 1) {
+        if (e & 1)
+            r = r * b % p;
+        b = b * b % p;
+    }
+    out[i] = make_uint2((uint32_t)r, (uint32_t)((r << 32) / p));
+}
+
+__global__ void fill_uniform_u32_kernel(uint32_t *out, size_t count, uint64_t seed, uint32_t p) {
+    const uint64_t limit = (1ull << 32) - ((1ull << 32) % p);
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+        uint64_t x = 0;
+        for (uint64_t a = 0;; ++a) {
+            x = sm64_draw(seed, i, a) >> 32;
+            if (x < limit)
+                break;
+        }
+        out[i] = (uint32_t)(x % p);
+    }
+}
+
+// One radix-2 Stockham DIF stage (ntt_cpu.cpp:66-79). Butterfly m < n/2:
+// l = v[m], r = v[m + n/2], J = 2^stage, s = m >> stage, j = m mod J,
+// y[2sJ + j] = l + r, y[(2s+1)J + j] = w_(J s) (l - r).
+__device__ __forceinline__ int32_t ref_modulo(int32_t x, int32_t mod) {
+    int32_t r = x % mod;  // truncates toward zero, as in C++
+    return r >= 0 ? r : r + mod;
+}
+
+__global__ void stage_u32_kernel(const uint32_t *in, uint32_t *out, const void *tw, uint32_t log_n, uint32_t stage,
+                                 uint32_t p, int wrap, uint64_t total) {
+    const uint64_t gid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= total)
+        return;
+    const uint64_t half = 1ull << (log_n - 1);
+    const uint64_t b = gid >> (log_n - 1), m = gid & (half - 1);
+    const uint64_t base = b << log_n;
+    const uint64_t J = 1ull << stage, s = m >> stage, j = m & (J - 1);
+    const uint64_t o0 = base + 2 * s * J + j, o1 = o0 + J;
+    if (wrap) {
+        // the reference's int32 arithmetic: the product wraps modulo 2^32
+        const int32_t *tw32 = static_cast<const int32_t *>(tw);
+        const int32_t l = (int32_t)in[base + m], r = (int32_t)in[base + m + half];
+        const int32_t w = tw32[J * s];
+        const int32_t md = (int32_t)p;
+        out[o0] = (uint32_t)ref_modulo(l + r, md);
+        const int32_t d = ref_modulo(l - r, md);
+        out[o1] = (uint32_t)ref_modulo((int32_t)((uint32_t)w * (uint32_t)d), md);
+    } else {
+        FieldU32 f;
+        f.p = p;
+        const uint2 w = static_cast<const uint2 *>(tw)[J * s];
+        const uint32_t l = in[base + m], r = in[base + m + half];
+        out[o0] = f.add(l, r);
+        out[o1] = f.mul_tw(f.sub(l, r), w);
+    }
+}
+
+cudaError_t launch_stage_u32(const void *in, void *out, const void *tw, uint32_t log_n, uint32_t stage, uint32_t p,
+                             int wrap, uint64_t batch, cudaStream_t s) {
+    const uint64_t total = batch << (log_n - 1);
+    const unsigned threads = 256;
+    const uint64_t blocks = (total + threads - 1) / threads;
+    if (blocks == 0)
+        return cudaSuccess;
+    stage_u32_kernel<<<(unsigned)blocks, threads, 0, s>>>(static_cast<const uint32_t *>(in),
+                                                           static_cast<uint32_t *>(out), tw, log_n, stage, p, wrap,
+                                                           total);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tile_u32(const PassDesc &d, uint32_t p, const void *tables, const void *in, void *out,
+                            uint64_t batch, cudaStream_t s) {
+    return launch_tile_t<FieldU32>(d, p, tables, in, out, batch, s);
+}
+
+cudaError_t gen_powers_u32(void *out, uint64_t count, uint64_t base, uint64_t scale, uint32_t p, cudaStream_t s) {
+    const unsigned threads = 256;
+    const uint64_t blocks = (count + threads - 1) / threads;
+    if (!blocks)
+        return cudaSuccess;
+    gen_powers_kernel<FieldU32><<<(unsigned)blocks, threads, 0, s>>>(static_cast<uint2 *>(out), count, base, scale,
+                                                                     p);
+    return cudaGetLastError();
+}
+
+cudaError_t pointwise_u32(const void *a, const void *b, void *out, size_t count, uint32_t p, cudaStream_t s) {
+    pointwise_kernel<FieldU32><<<grid_for(count, 256), 256, 0, s>>>(
+        static_cast<const uint32_t *>(a), static_cast<const uint32_t *>(b), static_cast<uint32_t *>(out), count, p);
+    return cudaGetLastError();
+}
+
+cudaError_t fill_uniform_u32(void *out, size_t count, uint64_t seed, uint32_t p, cudaStream_t s) {
+    fill_uniform_u32_kernel<<<grid_for(count, 256), 256, 0, s>>>(static_cast<uint32_t *>(out), count, seed, p);
+    return cudaGetLastError();
+}
+
+cudaError_t copy_scale_u32(const void *in, void *out, size_t count, uint64_t scale_tw, uint32_t p, cudaStream_t s) {
+    copy_scale_kernel<FieldU32><<<grid_for(count, 256), 256, 0, s>>>(static_cast<const uint32_t *>(in),
+                                                                     static_cast<uint32_t *>(out), count, scale_tw,
+                                                                     p);
+    return cudaGetLastError();
+}
+
+}  // namespace stntt

@@ -1,0 +1,230 @@
+// tile.cuh -- the NTT tile kernel: C independent DFTs of length L per CTA.
+//
+// One kernel covers every HBM pass of the transform:
+//   ROW pass: C rows, each contiguous in memory, written to a strided
+//     (digit-reversed) position. With n == L this is the whole transform
+//     of small sizes (the reference's stNttRadix2 / stNttRadix2Adaptive,
+//     src/cuda/ntt/implementations/st_ntt_radix2*.cuh); with n > L it is the
+//     last four-step pass.
+//   COL pass: C adjacent columns at stride S, followed by the four-step
+//     twiddle w_M^(col*k) (and n^-1 for the first inverse pass).
+// Together they replace the reference's log2(n)-10 one-stage-per-launch
+// passes (stNttGlobalRadix2_first/_rest, st_ntt_global_radix2.cuh:8-117) and
+// the in-block stNttLocalRadix2 (st_ntt_local_radix2.cuh:5-110) with 1-3
+// HBM passes.
+//
+// Inside a tile: radix-16 Stockham DIT steps (one leading radix-2/4/8 step
+// when log2 L is not a multiple of 4). A step reads R values per item into
+// registers, applies w_(R p)^(r k), runs an R-point DFT as a radix-2 network
+// in registers, and writes to shared memory in Stockham order. The first
+// step reads HBM directly and the last writes HBM directly, so each element
+// crosses HBM once per pass. Shared memory is padded (one element per 32
+// for 4-byte, per 16 for 8-byte values) so the Stockham patterns avoid bank
+// conflicts.
+#pragma once
+#include <cstdint>
+
+#include "fields.cuh"
+#include "internal.h"
+
+namespace stntt {
+
+template <class F>
+struct TileArgs {
+    using T = typename F::T;
+    using TW = typename F::TW;
+    const T *in;
+    T *out;
+    const TW *twL;     // w_L^e, e < L
+    const TW *tw4_lo;  // COL: w_M^e, e < 2^h
+    const TW *tw4_hi;  // COL: s * w_M^(e * 2^h), e < M / 2^h  (s = n^-1 on the first inverse pass)
+    TW wR[8];          // w_16^j (for L < 16: entry j*16/L holds w_L^j)
+    TW scale;          // ROW with do_scale: n^-1
+    uint32_t p;
+    uint32_t logL, logC, mode, do_scale, tfast, h;
+    uint32_t logN;          // elements per transform
+    uint32_t logM, logS;    // COL: sub-problem size, column stride
+    uint32_t logN1, logN2;  // ROW: rows r map to input row ((r mod n1) * n2 + r / n1)
+    uint32_t cs;            // shared-memory column stride, elements
+    uint64_t total;         // columns (COL) or rows (ROW) over the whole batch
+};
+
+template <class F>
+struct Pad;
+template <>
+struct Pad<FieldU32> {
+    static __device__ __forceinline__ uint32_t at(uint32_t i) { return i + (i >> 5); }
+};
+template <>
+struct Pad<FieldGL> {
+    static __device__ __forceinline__ uint32_t at(uint32_t i) { return i + (i >> 4); }
+};
+
+template <int LOGR>
+__host__ __device__ constexpr int bit_reverse(int r) {
+    int y = 0;
+    for (int i = 0; i < LOGR; ++i)
+        y |= ((r >> i) & 1) << (LOGR - 1 - i);
+    return y;
+}
+
+// R-point DFT with root w_R, as a radix-2 DIF network: natural order in,
+// bit-reversed order out. Span-2h stages use w_(2h)^j = w_16^(j*16/(2h)).
+template <class F, int R>
+__device__ __forceinline__ void dft_reg(const F &f, typename F::T *x, const typename F::TW *w16) {
+#pragma unroll
+    for (int h = R / 2; h >= 1; h >>= 1) {
+#pragma unroll
+        for (int base = 0; base < R; base += 2 * h) {
+#pragma unroll
+            for (int j = 0; j < h; ++j) {
+                const typename F::T a = x[base + j], b = x[base + j + h];
+                x[base + j] = f.add(a, b);
+                const typename F::T d = f.sub(a, b);
+                x[base + j + h] = (j == 0) ? d : f.mul_tw(d, w16[j * (16 / (2 * h))]);
+            }
+        }
+    }
+}
+
+struct Geo {
+    uint64_t ibase, istride, obase, ostride, col;
+    bool valid;  // false for the padding rows of a partial last CTA
+};
+
+template <class F, int E, int LOGR, bool first, bool last>
+__device__ __forceinline__ void tile_step(const TileArgs<F> &a, const F &f, typename F::T (&x)[E],
+                                          typename F::T *sm, uint32_t c, uint32_t u, uint32_t logp, const Geo &g) {
+    using T = typename F::T;
+    constexpr int R = 1 << LOGR, ITEMS = E / R;
+    const uint32_t L = 1u << a.logL, U = L / E, T_ = L >> LOGR;
+    const uint32_t pm = (1u << logp) - 1;
+    T *col_sm = sm + c * a.cs;
+
+    // ---- read R inputs per item: idx = t + r * L/R
+#pragma unroll
+    for (int m = 0; m < ITEMS; ++m) {
+        const uint32_t t = u + m * U;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const uint32_t idx = t + r * T_;
+            if constexpr (first)
+                x[m * R + r] = g.valid ? a.in[g.ibase + (uint64_t)idx * g.istride] : T(0);
+            else
+                x[m * R + r] = col_sm[Pad<F>::at(idx)];
+        }
+    }
+    // ---- twiddle w_(R p)^(r k) = w_L^(r k L/(R p)), k = t mod p; then R-point DFT
+#pragma unroll
+    for (int m = 0; m < ITEMS; ++m) {
+        const uint32_t t = u + m * U;
+        if constexpr (!first) {
+            const uint32_t k = t & pm;
+            const uint32_t sh = a.logL - LOGR - logp;
+#pragma unroll
+            for (int r = 1; r < R; ++r)
+                x[m * R + r] = f.mul_tw(x[m * R + r], __ldg(&a.twL[(r * k) << sh]));
+        }
+        dft_reg<F, R>(f, &x[m * R], a.wR);
+    }
+    if constexpr (!first && !last)
+        __syncthreads();  // every read of this step precedes any write
+    // ---- write output r of item t to (t - k) R + k + r p
+#pragma unroll
+    for (int m = 0; m < ITEMS; ++m) {
+        const uint32_t t = u + m * U;
+        const uint32_t k = t & pm;
+        const uint32_t base = ((t - k) << LOGR) + k;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const uint32_t pos = base + ((uint32_t)r << logp);
+            T v = x[m * R + bit_reverse<LOGR>(r)];
+            if constexpr (last) {
+                if (a.mode == kModeCol) {
+                    const uint64_t e = g.col * pos;
+                    const uint32_t lo = (uint32_t)(e & ((1ull << a.h) - 1));
+                    const uint32_t hi = (uint32_t)(e >> a.h);
+                    v = f.mul_tw(f.mul_tw(v, __ldg(&a.tw4_lo[lo])), __ldg(&a.tw4_hi[hi]));
+                } else if (a.do_scale) {
+                    v = f.mul_tw(v, a.scale);
+                }
+                if (g.valid)
+                    a.out[g.obase + (uint64_t)pos * g.ostride] = v;
+            } else {
+                col_sm[Pad<F>::at(pos)] = v;
+            }
+        }
+    }
+    if constexpr (!last)
+        __syncthreads();
+}
+
+template <class F, int E, int TAIL>
+__global__ void __launch_bounds__(E >= 32 ? 512 : 1024) tile_kernel(const TileArgs<F> a) {
+    using T = typename F::T;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *sm = reinterpret_cast<T *>(smem_raw);
+    F f;
+    f.p = a.p;
+
+    const uint32_t C = 1u << a.logC;
+    constexpr uint32_t logE = E >= 32 ? 5 : E >= 16 ? 4 : E >= 8 ? 3 : E >= 4 ? 2 : 1;
+    const uint32_t logU = a.logL - logE;  // log2(L / E): threads per column
+    uint32_t c, u;
+    if (a.tfast) {
+        u = threadIdx.x & ((1u << logU) - 1);
+        c = threadIdx.x >> logU;
+    } else {
+        c = threadIdx.x & (C - 1);
+        u = threadIdx.x >> a.logC;
+    }
+    const uint64_t gi = ((uint64_t)blockIdx.x << a.logC) + c;
+    const uint32_t logPer = a.logN - a.logL;
+    const uint64_t b = gi >> logPer;
+    const uint64_t rem = gi & ((1ull << logPer) - 1);
+    const uint64_t tbase = b << a.logN;
+    Geo g;
+    g.valid = gi < a.total;
+    if (a.mode == kModeCol) {
+        const uint64_t q = rem >> a.logS;
+        g.col = rem & ((1ull << a.logS) - 1);
+        g.ibase = g.obase = tbase + (q << a.logM) + g.col;
+        g.istride = g.ostride = 1ull << a.logS;
+    } else {
+        const uint64_t inrow = ((rem & ((1ull << a.logN1) - 1)) << a.logN2) + (rem >> a.logN1);
+        g.col = 0;
+        g.ibase = tbase + (inrow << a.logL);
+        g.istride = 1;
+        g.obase = tbase + rem;
+        g.ostride = 1ull << logPer;
+    }
+
+    T x[E];
+    const int n16 = (int)(a.logL >> 2);  // radix-16 steps after the optional leading step
+    uint32_t logp = 0;
+    if constexpr (TAIL > 0) {
+        if (n16 == 0) {
+            tile_step<F, E, TAIL, true, true>(a, f, x, sm, c, u, 0, g);
+            return;
+        }
+        tile_step<F, E, TAIL, true, false>(a, f, x, sm, c, u, 0, g);
+        logp = TAIL;
+    } else {
+        if (n16 == 1) {
+            tile_step<F, E, 4, true, true>(a, f, x, sm, c, u, 0, g);
+            return;
+        }
+        tile_step<F, E, 4, true, false>(a, f, x, sm, c, u, 0, g);
+        logp = 4;
+    }
+    if constexpr (E >= 16) {
+        const int mid = n16 - (TAIL > 0 ? 1 : 2);  // radix-16 steps between the first and the last
+        for (int s = 0; s < mid; ++s) {
+            tile_step<F, E, 4, false, false>(a, f, x, sm, c, u, logp, g);
+            logp += 4;
+        }
+        tile_step<F, E, 4, false, true>(a, f, x, sm, c, u, logp, g);
+    }
+}
+
+}  // namespace stntt

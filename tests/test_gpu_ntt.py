@@ -1,0 +1,339 @@
+"""GPU parity: the CUDA library (through its C ABI) against the CPU oracle and
+the reference's own vectors. Bit-exact everywhere (integer arithmetic).
+
+Cases follow the reference suite (src/tests/cuda/ntt/st_ntt_test.cu:51-97):
+util::Rng(42) inputs in [0,9], n = 2^2..2^20 x batches {1,2,5,10}, and the
+suite's skipped 2^21..2^26 range; plus uniform residues in [0,p) for both
+fields, schoolbook DFT at small n, round trips and linearity at full size.
+"""
+
+import hashlib
+
+import numpy as np
+import pytest
+
+import oracle as O
+import stntt_gb300 as st
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).astype("<i4").tobytes()).hexdigest()
+
+
+def dev32(a):
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.uint32).view(np.int32).copy()).cuda()
+
+
+def host32(t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy().view(np.uint32)
+
+
+def dev64(a):
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.uint64).view(np.int64).copy()).cuda()
+
+
+def host64(t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy().view(np.uint64)
+
+
+@pytest.fixture(scope="module")
+def ref_stream():
+    return O.ref_rng_vector(10 << 20)
+
+
+# --------------------------------------------------------------- 32-bit field
+def test_reference_suite_exact(ctx, golden, ref_stream):
+    """GPU == oracle (exact field) on every reference-suite case; for n <= 2^13
+    also == the unmodified reference output."""
+    for case in golden["stockham"]:
+        lg, b = case["log_n"], case["batch"]
+        if lg > 20:
+            continue
+        n = 1 << lg
+        x = ref_stream[: n * b].astype(np.uint32)
+        d = dev32(x)
+        ctx.ntt_u32(d, lg, b, case["mod"], case["root"])
+        got = host32(d)
+        want = O.ntt_u32(x, case["root"], case["mod"], batch=b)
+        assert np.array_equal(got, want), (lg, b)
+        if lg <= 13:
+            assert sha(got.view(np.int32)) == case["sha256"], (lg, b)
+
+
+def test_reference_suite_ref_wrap(ctx, golden, ref_stream):
+    """STNTT_FLAG_REF_WRAP reproduces the reference bit for bit at every n,
+    including the suite's skipped 2^21..2^26 range."""
+    big = O.ref_rng_vector(1 << 26)
+    for case in golden["stockham"]:
+        lg, b = case["log_n"], case["batch"]
+        n = 1 << lg
+        src = ref_stream if n * b <= ref_stream.size else big
+        d = dev32(src[: n * b].astype(np.uint32))
+        ctx.ntt_u32(d, lg, b, case["mod"], case["root"], ref_wrap=True)
+        assert sha(host32(d).view(np.int32)) == case["sha256"], (lg, b)
+
+
+def test_host_api_mirrors_nttStockham(golden, ref_stream, stntt_lib):
+    """st.nttStockham(int32 host array, size, root, mod, batches) in place,
+    as src/ntt/ntt_cpu.h:8-9."""
+    for case in golden["stockham"]:
+        lg, b = case["log_n"], case["batch"]
+        if lg > 16:
+            continue
+        v = ref_stream[: (1 << lg) * b].copy()
+        st.nttStockham(v, 1 << lg, case["root"], case["mod"], b, ref_wrap=True)
+        assert sha(v) == case["sha256"], (lg, b)
+        if lg <= 13:
+            w = ref_stream[: (1 << lg) * b].copy()
+            st.nttStockham(w, 1 << lg, case["root"], case["mod"], b)
+            assert sha(w) == case["sha256"], (lg, b)
+    with pytest.raises(st.StnttError, match="must be a power of 2"):
+        st.nttStockham(np.zeros(12, np.int32), 12, 1, 13)
+
+
+@pytest.mark.parametrize("lg", list(range(0, 23)))
+def test_u32_uniform_vs_oracle(ctx, lg):
+    p, root = st.params_u32(lg)
+    b = max(1, (1 << 16) >> lg)
+    x = O.uniform_u32(100 + lg, p, b << lg)
+    d = dev32(x)
+    ctx.ntt_u32(d, lg, b, p, root)
+    f = host32(d)
+    assert np.array_equal(f, O.ntt_u32(x, root, p, batch=b)), lg
+    ctx.ntt_u32(d, lg, b, p, root, inverse=True)
+    assert np.array_equal(host32(d), x), lg
+
+
+@pytest.mark.parametrize("lg", [1, 4, 7, 10])
+def test_u32_schoolbook(ctx, lg):
+    p, root = st.params_u32(lg)
+    x = O.uniform_u32(7 + lg, p, 1 << lg)
+    d = dev32(x)
+    ctx.ntt_u32(d, lg, 1, p, root)
+    assert np.array_equal(host32(d), O.dft_u32(x, root, p))
+
+
+def test_u32_inverse_vs_oracle(ctx):
+    for lg in (3, 9, 13, 14, 19):
+        p, root = st.params_u32(lg)
+        x = O.uniform_u32(55, p, 2 << lg)
+        d = dev32(x)
+        ctx.ntt_u32(d, lg, 2, p, root, inverse=True)
+        assert np.array_equal(host32(d), O.ntt_u32(x, root, p, inverse=True, batch=2)), lg
+
+
+def _dft_at(x, w, k, p):
+    """X[k] = sum_j x_j w^(jk) mod p for one k (vectorised, p < 2^32)."""
+    n = x.size
+    B = 1 << ((n.bit_length() - 1 + 1) // 2)
+    wk = pow(w, k, p)
+    lo = np.empty(B, np.uint64)
+    acc = 1
+    for i in range(B):
+        lo[i] = acc
+        acc = acc * wk % p
+    hi = np.empty(n // B, np.uint64)
+    step = pow(wk, B, p)
+    acc = 1
+    for i in range(n // B):
+        hi[i] = acc
+        acc = acc * step % p
+    pw = (hi[:, None] * lo[None, :]) % np.uint64(p)
+    return int(((x.astype(np.uint64).reshape(-1, B) * pw) % np.uint64(p)).sum() % p)
+
+
+@pytest.mark.parametrize("lg", [24, 26])
+def test_u32_full_size(ctx, lg):
+    """u32 2^24 vs the oracle; u32 2^26: spot DFT values, linearity, round trip."""
+    p, root = st.params_u32(lg)
+    n = 1 << lg
+    x = O.uniform_u32(31, p, n)
+    d = dev32(x)
+    ctx.ntt_u32(d, lg, 1, p, root)
+    f = host32(d)
+    if lg <= 24:
+        assert np.array_equal(f, O.ntt_u32(x, root, p))
+    for k in (0, 1, 12345, n - 1):
+        assert int(f[k]) == _dft_at(x, root, k, p), k
+    y = O.uniform_u32(32, p, n)
+    dy = dev32(y)
+    ctx.ntt_u32(dy, lg, 1, p, root)
+    s = dev32((x.astype(np.uint64) + y) % p)
+    ctx.ntt_u32(s, lg, 1, p, root)
+    assert np.array_equal(host32(s), ((f.astype(np.uint64) + host32(dy)) % p).astype(np.uint32))
+    ctx.ntt_u32(d, lg, 1, p, root, inverse=True)
+    assert np.array_equal(host32(d), x)
+
+
+def test_u32_partial_steps(ctx):
+    """The nsteps hook (ntt_cpu.h:8): first k radix-2 stages, exact and wrap."""
+    for lg in (5, 11, 16):
+        p, root = st.params_u32(lg)
+        x = O.uniform_u32(3, p, 1 << lg)
+        for k in (0, 1, lg // 2, lg):
+            d = dev32(x)
+            ctx.ntt_u32_steps(d, lg, 1, p, root, k)
+            want = x.copy()
+            O.lib().orc_ntt_u32(want, 1 << lg, root, p, k)
+            assert np.array_equal(host32(d), want), (lg, k)
+            d = dev32(x)
+            ctx.ntt_u32_steps(d, lg, 1, p, root, k, ref_wrap=True)
+            w2 = O.ntt_ref_wrap(x.view(np.int32), root, p, nsteps=k)
+            assert np.array_equal(host32(d).view(np.int32), w2), (lg, k)
+
+
+# --------------------------------------------------------------- Goldilocks
+@pytest.mark.parametrize("lg", list(range(0, 23)))
+def test_gl64_vs_oracle(ctx, lg):
+    b = max(1, (1 << 14) >> lg)
+    x = O.uniform_u64(500 + lg, b << lg)
+    d = dev64(x)
+    ctx.ntt_gl64(d, lg, b)
+    f = host64(d)
+    assert np.array_equal(f, O.ntt_gl64(x, batch=b)), lg
+    ctx.ntt_gl64(d, lg, b, inverse=True)
+    assert np.array_equal(host64(d), x), lg
+
+
+@pytest.mark.parametrize("lg", [1, 5, 8, 10])
+def test_gl64_schoolbook(ctx, lg):
+    x = O.uniform_u64(77 + lg, 1 << lg)
+    d = dev64(x)
+    ctx.ntt_gl64(d, lg)
+    assert np.array_equal(host64(d), O.dft_gl64(x, O.gl_root(lg)))
+
+
+def test_gl64_inverse_vs_oracle(ctx):
+    for lg in (2, 12, 13, 17, 20):
+        x = O.uniform_u64(66, 3 << lg)
+        d = dev64(x)
+        ctx.ntt_gl64(d, lg, 3, inverse=True)
+        assert np.array_equal(host64(d), O.ntt_gl64(x, inverse=True, batch=3)), lg
+
+
+def test_gl64_2e24(ctx):
+    """The headline size: Goldilocks 2^24, forward vs oracle, round trip."""
+    lg = 24
+    x = O.uniform_u64(2024, 1 << lg)
+    d = dev64(x)
+    ctx.ntt_gl64(d, lg)
+    f = host64(d)
+    assert np.array_equal(f, O.ntt_gl64(x, threads=1))
+    ctx.ntt_gl64(d, lg, inverse=True)
+    assert np.array_equal(host64(d), x)
+
+
+def test_gl64_out_of_place(ctx):
+    for lg in (6, 15):
+        x = O.uniform_u64(4, 1 << lg)
+        src = dev64(x)
+        dst = torch.zeros_like(src)
+        ctx.ntt_gl64_oop(src, dst, lg)
+        assert np.array_equal(host64(src), x)
+        assert np.array_equal(host64(dst), O.ntt_gl64(x))
+
+
+# --------------------------------------------------------------- polymul
+@pytest.mark.parametrize("lg", [1, 6, 12])
+def test_polymul_u32_vs_schoolbook(ctx, lg):
+    p, root = st.params_u32(lg)
+    n = 1 << lg
+    h = max(1, n // 2)
+    a = np.zeros(n, np.uint32)
+    b = np.zeros(n, np.uint32)
+    a[:h] = O.uniform_u32(1, p, h)
+    b[:h] = O.uniform_u32(2, p, h)
+    da, db = dev32(a), dev32(b)
+    out = torch.empty_like(da)
+    ctx.polymul_u32(da, db, out, lg, p, root)
+    want = O.polymul_u32(a[:h], b[:h], p)
+    got = host32(out)
+    assert np.array_equal(got[: want.size], want)
+    assert not got[want.size:].any()
+
+
+@pytest.mark.parametrize("lg", [1, 6, 12])
+def test_polymul_gl64_vs_schoolbook(ctx, lg):
+    n = 1 << lg
+    h = max(1, n // 2)
+    a = np.zeros(n, np.uint64)
+    b = np.zeros(n, np.uint64)
+    a[:h] = O.uniform_u64(3, h)
+    b[:h] = O.uniform_u64(4, h)
+    da, db = dev64(a), dev64(b)
+    ctx.polymul_gl64(da, db, da, lg)  # output aliases an input
+    want = O.polymul_gl64(a[:h], b[:h])
+    got = host64(da)
+    assert np.array_equal(got[: want.size], want)
+
+
+def test_pwc_convolution_semantics(ctx, golden):
+    """pwc_convolution (ntt_cpu.cpp:180-193): cyclic product with p >= max^2*len+1."""
+    for c in golden["pwc"]:
+        n = len(c["a"])
+        lg = n.bit_length() - 1
+        root, mod = st.findParams(n, max(max(c["a"]), max(c["b"])) ** 2 * n + 1)
+        assert (root, mod) == (c["root"], c["mod"])
+        da, db = dev32(np.array(c["a"], np.uint32)), dev32(np.array(c["b"], np.uint32))
+        out = torch.empty_like(da)
+        ctx.polymul_u32(da, db, out, lg, mod, root)
+        assert host32(out).tolist() == c["out"], n
+
+
+# --------------------------------------------------------------- batches, inputs, errors
+def test_batch_jobs_match_single_calls(ctx):
+    rng = np.random.default_rng(5)
+    jobs, bufs, want = [], [], []
+    for i in range(24):
+        lg = int(rng.integers(1, 16))
+        inv = i % 2
+        if i % 3 == 0:
+            p, root = st.params_u32(lg)
+            x = O.uniform_u32(i, p, 1 << lg)
+            d = dev32(x)
+            jobs.append(st.Job(st.FIELD_U32, lg, inv, p, root, 0, d.data_ptr()))
+            want.append(O.ntt_u32(x, root, p, inverse=bool(inv)))
+        else:
+            x = O.uniform_u64(i, 1 << lg)
+            d = dev64(x)
+            jobs.append(st.Job(st.FIELD_GL64, lg, inv, 0, 0, 0, d.data_ptr()))
+            want.append(O.ntt_gl64(x, inverse=bool(inv)))
+        bufs.append(d)
+    ctx.ntt_batch(jobs)
+    torch.cuda.synchronize()
+    for d, w in zip(bufs, want):
+        got = host32(d) if d.dtype == torch.int32 else host64(d)
+        assert np.array_equal(got, w)
+
+
+def test_device_input_generator_matches_host(stntt_lib):
+    t = torch.empty(70000, dtype=torch.int32, device="cuda")
+    st.fill_uniform_u32(t, 11, 469762049)
+    assert np.array_equal(host32(t), O.uniform_u32(11, 469762049, 70000))
+    g = torch.empty(70000, dtype=torch.int64, device="cuda")
+    st.fill_uniform_gl64(g, 12)
+    assert np.array_equal(host64(g), O.uniform_u64(12, 70000))
+
+
+def test_argument_errors(ctx):
+    d = torch.zeros(16, dtype=torch.int32, device="cuda")
+    with pytest.raises(st.StnttError, match="EINVAL"):
+        ctx.ntt_u32(d, 4, 1, 65537, 2)  # 2 is not a primitive 16th root mod 65537
+    with pytest.raises(st.StnttError, match="EINVAL"):
+        ctx.ntt_u32(d, 4, 1, 65536, 3)
+    with pytest.raises(st.StnttError, match="EUNSUPPORTED"):
+        ctx.ntt_u32(d, 28, 1, 65537, 3)
+    with pytest.raises(st.StnttError, match="EINVAL"):
+        ctx.ntt_u32(d, 4, 1, 65537, 3, inverse=True, ref_wrap=True)
+    g = torch.zeros(16, dtype=torch.int64, device="cuda")
+    with pytest.raises(st.StnttError, match="EUNSUPPORTED"):
+        ctx.ntt_gl64(g, 33)
+    # state stays usable
+    p, root = st.params_u32(4)
+    ctx.ntt_u32(d, 4, 1, p, root)
+    assert not host32(d).any()
