@@ -87,6 +87,19 @@ int stntt_prepare(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t p, uint32_
 int stntt_plan_info(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t p, uint32_t root, int dir,
                     uint32_t *passes, uint32_t *pass_logs);
 
+/* Override the plan for one (field, log_n): npasses HBM passes (1..4) with
+ * tile lengths 2^pass_logs[i] (summing to log_n, each <= 13; npasses <= 3), elements per
+ * thread elems[i] (16 or 32; 0 = default) and columns per CTA cols[i] (a power
+ * of two; 0 = default). Drops cached plans of that size. The autotuner
+ * (stntt_gb300/tune.py) drives this and stores its choices on disk.
+ * stntt_clear_plans() restores the built-in defaults for every size. */
+int stntt_set_plan(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t npasses, const uint32_t *pass_logs,
+                   const uint32_t *elems, const uint32_t *cols);
+int stntt_clear_plans(stntt_ctx *ctx);
+/* "name|SM count|driver version|compute capability" of a device: the key
+ * under which tuned plans are cached. */
+int stntt_device_key(int device, char *buf, size_t len);
+
 /* ---- transforms on device buffers ------------------------------------------ */
 /* In place, `batch` contiguous transforms of 2^log_n elements.
  * Replaces cuda::ntt::autoNtt<n>(NttArgs) (src/cuda/ntt/ntt_kernel.cuh:153-200)

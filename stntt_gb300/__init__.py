@@ -68,6 +68,9 @@ _SIGS = {
     "stntt_gl64_root": (_int, [_u32, C.POINTER(_u64)]),
     "stntt_prepare": (_int, [_vp, _int, _u32, _u32, _u32, _int]),
     "stntt_plan_info": (_int, [_vp, _int, _u32, _u32, _u32, _int, C.POINTER(_u32), C.POINTER(_u32)]),
+    "stntt_set_plan": (_int, [_vp, _int, _u32, _u32, C.POINTER(_u32), C.POINTER(_u32), C.POINTER(_u32)]),
+    "stntt_clear_plans": (_int, [_vp]),
+    "stntt_device_key": (_int, [_int, C.c_char_p, _sz]),
     "stntt_ntt_u32": (_int, [_vp, _vp, _u32, _u32, _u32, _u32, _int, _u32, _vp]),
     "stntt_ntt_gl64": (_int, [_vp, _vp, _u32, _u32, _int, _vp]),
     "stntt_ntt_u32_oop": (_int, [_vp, _vp, _vp, _u32, _u32, _u32, _u32, _int, _vp]),
@@ -138,6 +141,12 @@ def gl64_root(log_n: int) -> int:
     r = _u64()
     _check(lib().stntt_gl64_root(log_n, C.byref(r)))
     return r.value
+
+
+def device_key(device: int = 0) -> str:
+    buf = C.create_string_buffer(256)
+    _check(lib().stntt_device_key(device, buf, 256))
+    return buf.value.decode()
 
 
 def _log2(n: int) -> int:
@@ -216,6 +225,15 @@ class Context:
         _check(lib().stntt_plan_info(self._h, field, log_n, p, root, INVERSE if inverse else FORWARD,
                                      C.byref(n), logs), self._h)
         return n.value, list(logs)[: n.value]
+
+    def set_plan(self, field: int, log_n: int, pass_logs, elems=None, cols=None) -> None:
+        """Override the plan shape for one size (see stntt_set_plan)."""
+        k = len(pass_logs)
+        arr = lambda v: (_u32 * k)(*(v if v is not None else [0] * k))  # noqa: E731
+        _check(lib().stntt_set_plan(self._h, field, log_n, k, arr(pass_logs), arr(elems), arr(cols)), self._h)
+
+    def clear_plans(self) -> None:
+        _check(lib().stntt_clear_plans(self._h), self._h)
 
     # -- device transforms (torch tensors: int32 storage for u32, int64 for gl64)
     def ntt_u32(self, data, log_n: int, batch: int, p: int, root: int, inverse: bool = False,

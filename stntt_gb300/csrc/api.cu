@@ -151,6 +151,11 @@ struct DevBuf {
     size_t bytes = 0;
 };
 
+// A plan shape chosen by the caller (the autotuner) instead of the default.
+struct PlanSpec {
+    std::vector<uint32_t> logs, elems, cols;
+};
+
 }  // namespace
 
 struct stntt_ctx {
@@ -159,6 +164,7 @@ struct stntt_ctx {
     std::map<PlanKey, std::unique_ptr<Plan>> plans;
     std::map<std::tuple<uint32_t, uint32_t, uint32_t, int>, DevBuf> stage_tables;  // (log_n, p, root, wrap)
     std::map<cudaStream_t, DevBuf> workspaces;
+    std::map<std::pair<int, uint32_t>, PlanSpec> specs;  // (field, log_n) -> override
     cudaStream_t setup = nullptr;
     // host-buffer calls: one at a time, on their own stream and staging buffer
     std::mutex host_mu;
@@ -218,13 +224,17 @@ uint64_t fmul(int field, uint64_t a, uint64_t b, uint32_t p) {
 
 // Tile geometry for one pass: elements per thread E, columns per CTA C,
 // shared-memory column stride and size.
-void shape_pass(PassDesc &d, int field, uint64_t rows_per_transform, uint64_t col_limit) {
+void shape_pass(PassDesc &d, int field, uint64_t col_limit, uint32_t want_E, uint32_t want_C) {
     const uint32_t L = 1u << d.logL;
     d.E = L < 16 ? L : (L >= 4096 ? 32 : 16);
+    if (L >= 16 && (want_E == 16 || want_E == 32) && want_E <= L)
+        d.E = want_E;
     const uint32_t U = L / d.E;
     const uint32_t max_threads = d.E >= 32 ? 512 : 1024;
     uint64_t C;
-    if (d.mode == kModeRow && d.logN == d.logL) {
+    if (want_C) {
+        C = want_C;
+    } else if (d.mode == kModeRow && d.logN == d.logL) {
         C = std::max<uint64_t>(1, 256 / U);  // whole transforms per CTA: ~256 threads
     } else {
         C = std::min<uint64_t>(16, 16384 / L);
@@ -233,7 +243,9 @@ void shape_pass(PassDesc &d, int field, uint64_t rows_per_transform, uint64_t co
     C = std::min<uint64_t>(C, col_limit);
     C = std::min<uint64_t>(C, 64);
     C = std::max<uint64_t>(C, 1);
-    (void)rows_per_transform;
+    const size_t esz = field == kFieldGL ? 8 : 4;
+    while (C > 1 && C * (L + (L >> 4) + 32) * esz > 200 * 1024)  // shared-memory budget per CTA
+        C >>= 1;
     d.logC = ilog2(C);
     d.threads = (uint32_t)(C * U);
     const uint32_t padshift = field == kFieldGL ? 4 : 5;
@@ -249,7 +261,8 @@ void shape_pass(PassDesc &d, int field, uint64_t rows_per_transform, uint64_t co
 }
 
 // Build the pass list and the twiddle tables for one transform.
-int build_plan(stntt_ctx *ctx, Plan &pl, int field, uint32_t log_n, uint32_t p, uint64_t root_dir, int dir) {
+int build_plan(stntt_ctx *ctx, Plan &pl, int field, uint32_t log_n, uint32_t p, uint64_t root_dir, int dir,
+               const PlanSpec *spec) {
     pl.field = field;
     pl.log_n = log_n;
     pl.p = p;
@@ -258,7 +271,9 @@ int build_plan(stntt_ctx *ctx, Plan &pl, int field, uint32_t log_n, uint32_t p, 
     const uint64_t n = 1ull << log_n;
     const uint32_t single_max = 13, tile_max = 12;
     std::vector<uint32_t> logs;
-    if (log_n <= single_max) {
+    if (spec) {
+        logs = spec->logs;
+    } else if (log_n <= single_max) {
         logs.push_back(log_n);
     } else {
         const uint32_t K = (log_n + tile_max - 1) / tile_max;
@@ -316,7 +331,7 @@ int build_plan(stntt_ctx *ctx, Plan &pl, int field, uint32_t log_n, uint32_t p, 
             d.logN2 = K == 3 ? logs[1] : 0;
             col_limit = 1ull << 20;
         }
-        shape_pass(d, field, n >> d.logL, col_limit);
+        shape_pass(d, field, col_limit, spec ? spec->elems[i] : 0, spec ? spec->cols[i] : 0);
         pl.passes.push_back(d);
         done += d.logL;
     }
@@ -351,8 +366,13 @@ int get_plan(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t p, uint64_t roo
         return STNTT_OK;
     }
     auto pl = std::make_unique<Plan>();
+    PlanSpec spec;
+    auto sit = ctx->specs.find({field, log_n});
+    const bool has_spec = sit != ctx->specs.end();
+    if (has_spec)
+        spec = sit->second;
     ctx->mu.unlock();
-    int rc = build_plan(ctx, *pl, field, log_n, p, rd, dir);
+    int rc = build_plan(ctx, *pl, field, log_n, p, rd, dir, has_spec ? &spec : nullptr);
     ctx->mu.lock();
     if (rc != STNTT_OK) {
         if (pl->d_tables)
@@ -711,6 +731,75 @@ int stntt_plan_info(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t p, uint3
     if (pass_logs)
         for (size_t i = 0; i < pl->passes.size() && i < 4; ++i)
             pass_logs[i] = pl->passes[i].logL;
+    return STNTT_OK;
+}
+
+int stntt_set_plan(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t npasses, const uint32_t *pass_logs,
+                   const uint32_t *elems, const uint32_t *cols) {
+    if (!ctx || !pass_logs || npasses == 0 || npasses > 3)
+        return fail(ctx, STNTT_EINVAL, "set_plan: bad arguments");
+    if (field != STNTT_FIELD_U32 && field != STNTT_FIELD_GL64)
+        return fail(ctx, STNTT_EINVAL, "set_plan: unknown field");
+    PlanSpec s;
+    uint32_t sum = 0;
+    for (uint32_t i = 0; i < npasses; ++i) {
+        const uint32_t lg = pass_logs[i], e = elems ? elems[i] : 0, c = cols ? cols[i] : 0;
+        if (lg == 0 || lg > 13)
+            return fail(ctx, STNTT_EINVAL, "set_plan: each pass length must be 2^1..2^13");
+        if (e != 0 && e != 16 && e != 32)
+            return fail(ctx, STNTT_EINVAL, "set_plan: elems must be 0, 16 or 32");
+        if (c & (c - 1))
+            return fail(ctx, STNTT_EINVAL, "set_plan: cols must be 0 or a power of two");
+        s.logs.push_back(lg);
+        s.elems.push_back(e);
+        s.cols.push_back(c);
+        sum += lg;
+    }
+    if (sum != log_n)
+        return fail(ctx, STNTT_EINVAL, "set_plan: pass lengths must multiply to 2^log_n");
+    const int f = field == STNTT_FIELD_GL64 ? kFieldGL : kFieldU32;
+    DeviceGuard g(ctx->device);
+    cudaDeviceSynchronize();  // plans about to be freed may be in use
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->specs[{f, log_n}] = s;
+    for (auto it = ctx->plans.begin(); it != ctx->plans.end();) {
+        if (it->first.field == f && it->first.log_n == log_n) {
+            if (it->second->d_tables)
+                cudaFree(it->second->d_tables);
+            ctx->mem -= it->second->table_bytes;
+            it = ctx->plans.erase(it);
+        } else {
+            ++it;
+        }
+    }
+    return STNTT_OK;
+}
+
+int stntt_device_key(int device, char *buf, size_t len) {
+    if (!buf || len == 0)
+        return STNTT_EINVAL;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess)
+        return STNTT_EINVAL;
+    int drv = 0;
+    cudaDriverGetVersion(&drv);
+    snprintf(buf, len, "%s|%d|%d|%d.%d", prop.name, prop.multiProcessorCount, drv, prop.major, prop.minor);
+    return STNTT_OK;
+}
+
+int stntt_clear_plans(stntt_ctx *ctx) {
+    if (!ctx)
+        return STNTT_EINVAL;
+    DeviceGuard g(ctx->device);
+    cudaDeviceSynchronize();
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->specs.clear();
+    for (auto &kv : ctx->plans) {
+        if (kv.second->d_tables)
+            cudaFree(kv.second->d_tables);
+        ctx->mem -= kv.second->table_bytes;
+    }
+    ctx->plans.clear();
     return STNTT_OK;
 }
 

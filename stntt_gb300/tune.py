@@ -1,0 +1,178 @@
+"""Autotuner for transform plans: pass split, elements per thread, columns per CTA.
+
+For one (field, log_n) it enumerates plan shapes the library accepts
+(``stntt_set_plan``), times each forward transform with CUDA events on a
+buffer large enough to fill the GPU, keeps the fastest, and stores it in a
+JSON cache keyed by the device (name | SM count | driver | capability, from
+``stntt_device_key``). ``apply_cache(ctx)`` replays cached choices into a
+context. Extends the reference's manual sweep over block sizes
+(src/bench.cu:88-91, ntt_kernel.cuh:27).
+
+    python -m stntt_gb300.tune --field gl64 --log-n 16 20 24
+"""
+
+from __future__ import annotations
+
+import argparse
+import itertools
+import json
+import os
+import time
+from pathlib import Path
+from typing import Iterable
+
+import stntt_gb300 as st
+
+DEFAULT_CACHE = Path(os.environ.get("STNTT_TUNE_CACHE", str(Path.home() / ".cache" / "stntt_gb300" / "plans.json")))
+
+
+def splits(log_n: int, max_pass: int = 13) -> list[list[int]]:
+    out = []
+    if log_n <= max_pass:
+        out.append([log_n])
+    for a in range(max(1, log_n - max_pass), min(max_pass, log_n - 1) + 1):
+        out.append([a, log_n - a])
+    if log_n >= 18:
+        for a in range(6, max_pass + 1):
+            for b in range(6, max_pass + 1):
+                c = log_n - a - b
+                if 6 <= c <= max_pass:
+                    out.append([a, b, c])
+    return out
+
+
+def candidates(field: int, log_n: int, full: bool = False) -> Iterable[tuple[list[int], list[int], list[int]]]:
+    """Plan shapes to try. Without `full`, only even-ish splits are kept."""
+    sp = splits(log_n)
+    if not full:
+        two = sorted([s for s in sp if len(s) <= 2], key=lambda s: max(s) - min(s))[:3]
+        three = sorted([s for s in sp if len(s) == 3], key=lambda s: max(s) - min(s))[:1]
+        sp = two + three
+    for logs in sp:
+        L_min = 1 << min(logs)
+        for e in [e for e in (16, 32) if e <= L_min] or [0]:
+            per_pass = []
+            for lg in logs:
+                L = 1 << lg
+                if len(logs) == 1:
+                    per_pass.append([0])
+                else:
+                    cs = [c for c in (2, 4, 8, 16) if c * L <= (1 << 15)]
+                    per_pass.append(cs if full else cs[:3])
+            for combo in itertools.product(*per_pass):
+                yield logs, [e] * len(logs), list(combo)
+
+
+def _time_plan(ctx: st.Context, field: int, log_n: int, data, p: int, root: int, batch: int, reps: int) -> float:
+    import torch
+
+    run = (lambda: ctx.ntt_gl64(data, log_n, batch)) if field == st.FIELD_GL64 else \
+        (lambda: ctx.ntt_u32(data, log_n, batch, p, root))
+    run()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(reps):
+        run()
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) * 1e3 / reps  # microseconds per call
+
+
+def tune(ctx: st.Context, field: int, log_n: int, reps: int = 10, full: bool = False, verbose: bool = False):
+    """Return (best_spec, best_us, all_results) for one size; leaves the best plan set."""
+    import torch
+
+    batch = max(1, (1 << 24) >> log_n)
+    n = batch << log_n
+    if field == st.FIELD_GL64:
+        data = torch.empty(n, dtype=torch.int64, device=f"cuda:{ctx.device}")
+        st.fill_uniform_gl64(data, 99)
+        p = root = 0
+    else:
+        p, root = st.params_u32(log_n)
+        data = torch.empty(n, dtype=torch.int32, device=f"cuda:{ctx.device}")
+        st.fill_uniform_u32(data, 99, p)
+    results = []
+    for logs, es, cs in candidates(field, log_n, full):
+        try:
+            ctx.set_plan(field, log_n, logs, es, cs)
+            us = _time_plan(ctx, field, log_n, data, p, root, batch, reps)
+        except st.StnttError as e:
+            if verbose:
+                print("skip", logs, es, cs, e)
+            continue
+        results.append({"logs": logs, "E": es, "C": cs, "us": us, "batch": batch})
+        if verbose:
+            print(f"{logs} E={es} C={cs}: {us:.1f} us", flush=True)
+    results.sort(key=lambda r: r["us"])
+    best = results[0]
+    ctx.set_plan(field, log_n, best["logs"], best["E"], best["C"])
+    return best, results
+
+
+def _key(device: int) -> str:
+    return st.device_key(device)
+
+
+def load_cache(path: Path = DEFAULT_CACHE) -> dict:
+    try:
+        return json.loads(Path(path).read_text())
+    except (OSError, ValueError):
+        return {}
+
+
+def save_cache(cache: dict, path: Path = DEFAULT_CACHE) -> None:
+    path = Path(path)
+    path.parent.mkdir(parents=True, exist_ok=True)
+    tmp = path.with_suffix(".tmp")
+    tmp.write_text(json.dumps(cache, indent=1, sort_keys=True))
+    os.replace(tmp, path)
+
+
+def apply_cache(ctx: st.Context, path: Path = DEFAULT_CACHE) -> int:
+    """Set every cached plan for this device on `ctx`; returns how many."""
+    entries = load_cache(path).get(_key(ctx.device), {})
+    k = 0
+    for name, e in entries.items():
+        field_s, lg = name.split(":")
+        field = st.FIELD_GL64 if field_s == "gl64" else st.FIELD_U32
+        ctx.set_plan(field, int(lg), e["logs"], e["E"], e["C"])
+        k += 1
+    return k
+
+
+def record(ctx: st.Context, field: int, log_n: int, best: dict, path: Path = DEFAULT_CACHE) -> None:
+    cache = load_cache(path)
+    ent = cache.setdefault(_key(ctx.device), {})
+    ent[f"{'gl64' if field == st.FIELD_GL64 else 'u32'}:{log_n}"] = {
+        "logs": best["logs"], "E": best["E"], "C": best["C"], "us": best["us"], "batch": best["batch"],
+        "when": time.strftime("%Y-%m-%dT%H:%M:%SZ", time.gmtime())}
+    save_cache(cache, path)
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--field", choices=["gl64", "u32"], default="gl64")
+    ap.add_argument("--log-n", type=int, nargs="+", default=[20, 24])
+    ap.add_argument("--reps", type=int, default=10)
+    ap.add_argument("--full", action="store_true")
+    ap.add_argument("--cache", default=str(DEFAULT_CACHE))
+    ap.add_argument("--verbose", action="store_true")
+    ap.add_argument("--out", default=None, help="also write all timings here (JSON)")
+    args = ap.parse_args()
+    field = st.FIELD_GL64 if args.field == "gl64" else st.FIELD_U32
+    ctx = st.Context(0)
+    allres = {}
+    for lg in args.log_n:
+        best, res = tune(ctx, field, lg, args.reps, args.full, args.verbose)
+        record(ctx, field, lg, best, Path(args.cache))
+        allres[f"{args.field}:{lg}"] = res
+        print(json.dumps({"size": f"{args.field}:{lg}", "best": best, "candidates": len(res)}), flush=True)
+    if args.out:
+        Path(args.out).write_text(json.dumps(allres, indent=1))
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()
