@@ -167,6 +167,20 @@ int stntt_pointwise_mul_u32(const uint32_t *d_a, const uint32_t *d_b, uint32_t *
 int stntt_pointwise_mul_gl64(const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_out, size_t count,
                              stntt_stream stream);
 
+/* ---- allocation-free variant ------------------------------------------------------ */
+/* No counterpart in the reference. For callers that cannot call cudaMalloc
+ * (a memory pool that already owns HBM, a host runtime that manages device
+ * memory itself, a loop that cannot take an allocation's synchronisation):
+ * the same Goldilocks transform as stntt_ntt_gl64_oop, without a context and
+ * without allocating. Its between-pass buffer and twiddle tables live in a
+ * fixed array inside the library (8 MiB + 256 KiB per GPU, kept until exit),
+ * so batch * 2^log_n must be <= 2^20 (else STNTT_EUNSUPPORTED). All calls
+ * share that array: calls that overlap on the GPU race, so order them on one
+ * stream. The first call on a device looks up the array's address; make it
+ * before capturing a stream into a CUDA graph. d_in may equal d_out. */
+int stntt_ntt_gl64_noalloc(const uint64_t *d_in, uint64_t *d_out, uint32_t log_n, uint32_t batch, int dir,
+                           stntt_stream stream);
+
 /* ---- synthetic inputs ------------------------------------------------------------ */
 /* Uniform residues in [0,p) from a counter-based splitmix64 stream:
  * element i, attempt a: z = mix64(seed + 0x9E3779B97F4A7C15 * (i + (a << 40) + 1));

@@ -86,6 +86,7 @@ _SIGS = {
     "stntt_pointwise_mul_gl64": (_int, [_vp, _vp, _vp, _sz, _vp]),
     "stntt_fill_uniform_u32": (_int, [_vp, _sz, _u64, _u32, _vp]),
     "stntt_fill_uniform_gl64": (_int, [_vp, _sz, _u64, _vp]),
+    "stntt_ntt_gl64_noalloc": (_int, [_vp, _vp, _u32, _u32, _int, _vp]),
 }
 
 
