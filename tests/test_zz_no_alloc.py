@@ -59,10 +59,11 @@ def test_noalloc_matches_regular_entry_point(stntt_lib):
         big = torch.empty(1 << 21, dtype=torch.int64, device="cuda")
         assert fn(C.c_void_p(big.data_ptr()), C.c_void_p(big.data_ptr()), 21, 1, 0, C.c_void_p(stream)) == 5
         assert fn(C.c_void_p(big.data_ptr()), C.c_void_p(big.data_ptr()), 20, 2, 0, C.c_void_p(stream)) == 5
-        # a warm call does not take device memory
+        # a warm call does not take device memory (buffer sized for the 2^20 transform)
+        d20 = _dev(O.uniform_u64(9, 1 << 20))
         torch.cuda.synchronize()
         free0, _ = torch.cuda.mem_get_info()
-        assert fn(C.c_void_p(d.data_ptr()), C.c_void_p(d.data_ptr()), 20, 1, 1, C.c_void_p(stream)) == 0
+        assert fn(C.c_void_p(d20.data_ptr()), C.c_void_p(d20.data_ptr()), 20, 1, 1, C.c_void_p(stream)) == 0
         torch.cuda.synchronize()
         free1, _ = torch.cuda.mem_get_info()
         assert free1 == free0
