@@ -146,12 +146,31 @@ typedef struct stntt_job {
 } stntt_job;
 
 /* Many independent transforms of uneven sizes, fields and directions in one
- * persistent launch (plus one launch for the few jobs too large for it).
- * Extends the reference's uniform `batches` packing
- * (src/cuda/ntt/ntt_kernel.cuh:31-39). */
+ * persistent launch per field (jobs with log_n < 4 or needing three HBM
+ * passes run as ordinary launches after it). Extends the reference's uniform
+ * `batches` packing (src/cuda/ntt/ntt_kernel.cuh:31-39). Synchronous: builds
+ * the work list, launches on `stream`, waits, and returns STNTT_ETIMEOUT if a
+ * bounded device-side wait gave up. Job buffers must not overlap. */
 int stntt_ntt_batch(stntt_ctx *ctx, const stntt_job *jobs, size_t njobs, stntt_stream stream);
 /* Same jobs, one launch sequence per job (the comparison baseline). */
 int stntt_ntt_batch_per_call(stntt_ctx *ctx, const stntt_job *jobs, size_t njobs, stntt_stream stream);
+
+/* Reusable batch (for CUDA graphs): create builds twiddle tables, the work
+ * list and a private scratch buffer (synchronous, not inside a capture);
+ * launch only zeroes its counters and launches (capturable, repeatable);
+ * status reads the device error flag once the stream has completed. */
+typedef struct stntt_batch stntt_batch;
+int stntt_batch_create(stntt_ctx *ctx, const stntt_job *jobs, size_t njobs, stntt_batch **out);
+int stntt_batch_launch(stntt_batch *b, stntt_stream stream);
+int stntt_batch_status(stntt_batch *b);
+/* items: work items of the persistent launches; grid: their total blocks;
+ * fallback: jobs run as ordinary launches. */
+int stntt_batch_info(const stntt_batch *b, size_t *items, uint32_t *grid, size_t *fallback);
+int stntt_batch_destroy(stntt_batch *b);
+/* Launch the persistent kernel on one work item whose dependency nothing
+ * satisfies, with the given poll limit; returns STNTT_ETIMEOUT when the
+ * kernel's bounded wait gave up and reported it (the context stays usable). */
+int stntt_selftest_wait_timeout(stntt_ctx *ctx, uint32_t spin_limit);
 
 /* ---- polynomial multiplication (pwcNtt / pwc_convolution, ntt_cpu.cpp:167-193) */
 /* d_out = cyclic convolution of d_a and d_b, length 2^log_n, i.e. the product

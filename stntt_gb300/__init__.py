@@ -87,6 +87,12 @@ _SIGS = {
     "stntt_fill_uniform_u32": (_int, [_vp, _sz, _u64, _u32, _vp]),
     "stntt_fill_uniform_gl64": (_int, [_vp, _sz, _u64, _vp]),
     "stntt_ntt_gl64_noalloc": (_int, [_vp, _vp, _u32, _u32, _int, _vp]),
+    "stntt_batch_create": (_int, [_vp, C.POINTER(Job), _sz, C.POINTER(_vp)]),
+    "stntt_batch_launch": (_int, [_vp, _vp]),
+    "stntt_batch_status": (_int, [_vp]),
+    "stntt_batch_info": (_int, [_vp, C.POINTER(_sz), C.POINTER(_u32), C.POINTER(_sz)]),
+    "stntt_batch_destroy": (_int, [_vp]),
+    "stntt_selftest_wait_timeout": (_int, [_vp, _u32]),
 }
 
 
@@ -273,6 +279,18 @@ class Context:
         f = lib().stntt_ntt_batch_per_call if per_call else lib().stntt_ntt_batch
         _check(f(self._h, arr, len(jobs), _stream(stream)), self._h)
 
+    # -- reusable batches (CUDA-graph friendly)
+    def batch_create(self, jobs: Sequence[Job]) -> "Batch":
+        arr = (Job * len(jobs))(*jobs)
+        h = _vp()
+        _check(lib().stntt_batch_create(self._h, arr, len(jobs), C.byref(h)), self._h)
+        return Batch(self, h.value)
+
+    def selftest_wait_timeout(self, spin_limit: int) -> int:
+        """Status of a persistent launch whose only work item waits on a
+        counter nothing sets (expected: 4, STNTT_ETIMEOUT)."""
+        return lib().stntt_selftest_wait_timeout(self._h, spin_limit)
+
     # -- host arrays (synchronous)
     def ntt_stockham_host(self, vec: np.ndarray, size: int, root: int, mod: int, batches: int = 1,
                           nsteps: Optional[int] = None, ref_wrap: bool = False) -> np.ndarray:
@@ -291,6 +309,36 @@ class Context:
         _check(lib().stntt_ntt_gl64_host(self._h, vec.ctypes.data, log_n, batch, INVERSE if inverse else FORWARD),
                self._h)
         return vec
+
+
+class Batch:
+    """A ``stntt_batch``: the work list of one uneven batch, launchable many
+    times (``launch`` is capturable in a CUDA graph)."""
+
+    def __init__(self, ctx: Context, handle: int):
+        self.ctx, self._h = ctx, handle
+
+    def launch(self, stream=None) -> None:
+        _check(lib().stntt_batch_launch(self._h, _stream(stream)), self.ctx.handle)
+
+    def status(self) -> int:
+        return lib().stntt_batch_status(self._h)
+
+    def info(self) -> dict:
+        it, fb, gr = _sz(), _sz(), _u32()
+        _check(lib().stntt_batch_info(self._h, C.byref(it), C.byref(gr), C.byref(fb)))
+        return {"items": it.value, "grid": gr.value, "fallback_jobs": fb.value}
+
+    def close(self) -> None:
+        if self._h:
+            lib().stntt_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):  # pragma: no cover
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def nttStockham(vec: np.ndarray, size: int, root: int, mod: int, batches: int = 1,

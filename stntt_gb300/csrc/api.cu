@@ -36,6 +36,18 @@ cudaError_t fill_uniform_u32(void *, size_t, uint64_t, uint32_t, cudaStream_t);
 cudaError_t fill_uniform_gl64(void *, size_t, uint64_t, cudaStream_t);
 cudaError_t copy_scale_u32(const void *, void *, size_t, uint64_t, uint32_t, cudaStream_t);
 cudaError_t copy_scale_gl64(const void *, void *, size_t, uint64_t, cudaStream_t);
+size_t batch_args_size_u32();
+size_t batch_args_size_gl64();
+void batch_args_fill_u32(const PassDesc &, uint32_t, const void *, const unsigned long long *,
+                         const unsigned long long *, uint64_t, void *);
+void batch_args_fill_gl64(const PassDesc &, uint32_t, const void *, const unsigned long long *,
+                          const unsigned long long *, uint64_t, void *);
+cudaError_t batch_prepare_u32(size_t, int *);
+cudaError_t batch_prepare_gl64(size_t, int *);
+cudaError_t batch_launch_u32(const void *, const void *, unsigned long long, unsigned int *, void *, size_t, unsigned,
+                             unsigned, cudaStream_t);
+cudaError_t batch_launch_gl64(const void *, const void *, unsigned long long, unsigned int *, void *, size_t,
+                              unsigned, unsigned, cudaStream_t);
 
 static constexpr uint64_t GL_P = 0xFFFFFFFF00000001ull;
 typedef unsigned __int128 u128;
@@ -997,9 +1009,6 @@ int stntt_ntt_batch_per_call(stntt_ctx *ctx, const stntt_job *jobs, size_t njobs
     return STNTT_OK;
 }
 
-int stntt_ntt_batch(stntt_ctx *ctx, const stntt_job *jobs, size_t njobs, stntt_stream stream) {
-    return stntt_ntt_batch_per_call(ctx, jobs, njobs, stream);
-}
 
 int stntt_pointwise_mul_u32(const uint32_t *d_a, const uint32_t *d_b, uint32_t *d_out, size_t count, uint32_t p,
                             stntt_stream stream) {
@@ -1093,6 +1102,403 @@ int stntt_fill_uniform_gl64(uint64_t *d_out, size_t count, uint64_t seed, stntt_
         return STNTT_OK;
     return launch_fill_uniform(kFieldGL, d_out, count, seed, 0, (cudaStream_t)stream) == cudaSuccess ? STNTT_OK
                                                                                                      : STNTT_ECUDA;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Persistent batched launch (batch.cuh): host-side work list
+// ===========================================================================
+namespace {
+
+struct BatchItemH {  // layout of stntt::BatchItem
+    uint32_t args, wait_job, wait_count, signal_job;
+    uint64_t blk;
+};
+static_assert(sizeof(BatchItemH) == 24, "BatchItem layout");
+struct BatchCtlH {
+    unsigned long long next;
+    unsigned int error, timeouts;
+};
+
+constexpr unsigned kDefaultSpinLimit = 5000000;  // polls of ~200 ns: about one second
+
+struct BatchPart {
+    int field = 0;
+    void *d_buf = nullptr;
+    size_t args_off = 0, items_off = 0, counters_off = 0, ctl_off = 0, ptr_off = 0, bytes = 0;
+    unsigned long long nitems = 0;
+    uint32_t ncounters = 0;
+    size_t smem = 0;
+    unsigned grid = 0;
+};
+
+size_t args_size(int field) { return field == kFieldGL ? batch_args_size_gl64() : batch_args_size_u32(); }
+void args_fill(int field, const PassDesc &d, uint32_t p, const void *t, const unsigned long long *ip,
+               const unsigned long long *op, uint64_t total, void *dst) {
+    if (field == kFieldGL)
+        batch_args_fill_gl64(d, p, t, ip, op, total, dst);
+    else
+        batch_args_fill_u32(d, p, t, ip, op, total, dst);
+}
+
+// 512-thread tile shape for the persistent kernel: 16 elements per thread,
+// C = 8192 / L columns or rows.
+void batch_shape(PassDesc &d, int field) {
+    const uint32_t L = 1u << d.logL;
+    d.E = 16;
+    const uint32_t U = L / 16, C = 8192 / L;
+    d.logC = ilog2(C);
+    d.threads = C * U;
+    const uint32_t padshift = field == kFieldGL ? 4 : 5, banks = field == kFieldGL ? 16 : 32;
+    const uint32_t base = L + (L >> padshift);
+    const uint32_t want = d.tfast ? (U < banks ? U : 0) : (C < banks ? banks / C : 0);
+    d.cs = base + ((want + banks - base % banks) % banks);
+    d.smem_bytes = (size_t)C * d.cs * (field == kFieldGL ? 8 : 4);
+}
+
+}  // namespace
+
+struct stntt_batch {
+    stntt_ctx *ctx = nullptr;
+    std::vector<BatchPart> parts;
+    std::vector<stntt_job> fallback;
+    void *d_scratch = nullptr;
+    size_t scratch_bytes = 0;
+    unsigned spin_limit = kDefaultSpinLimit;
+};
+
+namespace {
+
+struct ClassKey {
+    uint32_t log_n, dir, p, root;
+    bool operator<(const ClassKey &o) const {
+        return std::tie(log_n, dir, p, root) < std::tie(o.log_n, o.dir, o.p, o.root);
+    }
+};
+
+int build_part(stntt_ctx *ctx, stntt_batch *bt, int field, const std::vector<const stntt_job *> &jobs,
+               size_t &scratch_cursor) {
+    std::map<ClassKey, std::vector<const stntt_job *>> classes;
+    for (const stntt_job *j : jobs)
+        classes[{j->log_n, j->dir, field == kFieldGL ? 0u : j->p, field == kFieldGL ? 0u : j->root}].push_back(j);
+    const size_t asz = args_size(field);
+    std::vector<unsigned char> args;                   // TileArgs, by value
+    std::vector<unsigned long long> ptrs;              // per-class data / scratch pointer arrays
+    std::vector<size_t> ptr_fix;                       // args records whose pointer fields are ptr offsets
+    std::vector<BatchItemH> phaseA, phaseB;
+    uint32_t njob2 = 0;
+    size_t smem = 0;
+    struct PendingArgs {
+        PassDesc d;
+        uint32_t p;
+        const void *tables;
+        size_t in_off, out_off;
+        uint64_t total;
+    };
+    std::vector<PendingArgs> pend;
+    for (auto &kv : classes) {
+        const ClassKey &ck = kv.first;
+        const auto &cj = kv.second;
+        const Plan *pl = nullptr;
+        uint64_t root = ck.root;
+        if (field == kFieldGL)
+            stntt_gl64_root(ck.log_n, &root);
+        int rc = get_plan(ctx, field, ck.log_n, ck.p, root, (int)ck.dir, &pl);
+        if (rc)
+            return rc;
+        const size_t J = cj.size();
+        const size_t data_off = ptrs.size();
+        for (const stntt_job *j : cj)
+            ptrs.push_back((unsigned long long)(uintptr_t)j->data);
+        if (pl->passes.size() == 1) {
+            PassDesc d = pl->passes[0];
+            d.tfast = 1;
+            batch_shape(d, field);
+            smem = std::max(smem, d.smem_bytes);
+            const uint32_t a_idx = (uint32_t)pend.size();
+            pend.push_back({d, ck.p, pl->d_tables, data_off, data_off, (uint64_t)J});
+            const uint64_t C = 1ull << d.logC;
+            for (uint64_t blk = 0; blk * C < J; ++blk)
+                phaseA.push_back({a_idx, ~0u, 0u, ~0u, blk});
+        } else {
+            // two passes: data -> scratch -> data
+            const size_t scr_off = ptrs.size();
+            const uint64_t n = 1ull << ck.log_n;
+            for (size_t i = 0; i < J; ++i) {
+                ptrs.push_back((unsigned long long)(uintptr_t)(static_cast<char *>(bt->d_scratch) + scratch_cursor));
+                scratch_cursor += n * (field == kFieldGL ? 8 : 4);
+            }
+            PassDesc d0 = pl->passes[0], d1 = pl->passes[1];
+            d0.tfast = 0;
+            d1.tfast = 0;
+            batch_shape(d0, field);
+            batch_shape(d1, field);
+            smem = std::max({smem, d0.smem_bytes, d1.smem_bytes});
+            const uint32_t a0 = (uint32_t)pend.size();
+            pend.push_back({d0, ck.p, pl->d_tables, data_off, scr_off, (uint64_t)J << (ck.log_n - d0.logL)});
+            const uint32_t a1 = (uint32_t)pend.size();
+            pend.push_back({d1, ck.p, pl->d_tables, scr_off, data_off, (uint64_t)J << (ck.log_n - d1.logL)});
+            const uint64_t per0 = 1ull << (ck.log_n - d0.logL - d0.logC);  // items per job, pass 0
+            const uint64_t per1 = 1ull << (ck.log_n - d1.logL - d1.logC);
+            for (size_t i = 0; i < J; ++i) {
+                const uint32_t job = njob2++;
+                for (uint64_t k = 0; k < per0; ++k)
+                    phaseA.push_back({a0, ~0u, 0u, job, i * per0 + k});
+                for (uint64_t k = 0; k < per1; ++k)
+                    phaseB.push_back({a1, job, (uint32_t)per0, ~0u, i * per1 + k});
+            }
+        }
+    }
+    BatchPart part;
+    part.field = field;
+    part.nitems = phaseA.size() + phaseB.size();
+    part.ncounters = std::max<uint32_t>(njob2, 1);
+    part.smem = smem;
+    // device layout: args | items | ptrs | counters | ctl
+    auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
+    part.args_off = 0;
+    part.items_off = al(pend.size() * asz);
+    part.ptr_off = al(part.items_off + part.nitems * sizeof(BatchItemH));
+    part.counters_off = al(part.ptr_off + ptrs.size() * sizeof(unsigned long long));
+    part.ctl_off = al(part.counters_off + part.ncounters * sizeof(unsigned int));
+    part.bytes = al(part.ctl_off + sizeof(BatchCtlH));
+    cudaError_t e = cudaMalloc(&part.d_buf, part.bytes);
+    if (e != cudaSuccess)
+        return fail(ctx, STNTT_ENOMEM, std::string("cudaMalloc(batch work list): ") + cudaGetErrorString(e));
+    bt->parts.push_back(part);
+    BatchPart &P = bt->parts.back();
+    std::vector<unsigned char> host(P.bytes, 0);
+    char *dbase = static_cast<char *>(P.d_buf);
+    const unsigned long long *dptrs = reinterpret_cast<const unsigned long long *>(dbase + P.ptr_off);
+    for (size_t i = 0; i < pend.size(); ++i)
+        args_fill(field, pend[i].d, pend[i].p, pend[i].tables, dptrs + pend[i].in_off, dptrs + pend[i].out_off,
+                  pend[i].total, host.data() + i * asz);
+    std::memcpy(host.data() + P.items_off, phaseA.data(), phaseA.size() * sizeof(BatchItemH));
+    std::memcpy(host.data() + P.items_off + phaseA.size() * sizeof(BatchItemH), phaseB.data(),
+                phaseB.size() * sizeof(BatchItemH));
+    std::memcpy(host.data() + P.ptr_off, ptrs.data(), ptrs.size() * sizeof(unsigned long long));
+    e = cudaMemcpy(P.d_buf, host.data(), P.bytes, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "batch work list upload");
+    int bps = 0;
+    e = field == kFieldGL ? batch_prepare_gl64(P.smem, &bps) : batch_prepare_u32(P.smem, &bps);
+    if (e != cudaSuccess || bps < 1)
+        return fail(ctx, STNTT_ECUDA, "batch kernel does not fit on an SM");
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    P.grid = (unsigned)std::min<unsigned long long>(P.nitems ? P.nitems : 1, (unsigned long long)sms * bps);
+    return STNTT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int stntt_batch_create(stntt_ctx *ctx, const stntt_job *jobs, size_t njobs, stntt_batch **out) {
+    if (!ctx || !out || (!jobs && njobs))
+        return STNTT_EINVAL;
+    *out = nullptr;
+    DeviceGuard g(ctx->device);
+    std::vector<const stntt_job *> by_field[2];
+    auto bt = std::make_unique<stntt_batch>();
+    bt->ctx = ctx;
+    size_t scratch_total = 0;
+    for (size_t i = 0; i < njobs; ++i) {
+        const stntt_job &j = jobs[i];
+        if (j.dir != STNTT_FORWARD && j.dir != STNTT_INVERSE)
+            return fail(ctx, STNTT_EINVAL, "job " + std::to_string(i) + ": bad direction");
+        if (!j.data)
+            return fail(ctx, STNTT_EINVAL, "job " + std::to_string(i) + ": null data");
+        int f;
+        uint32_t passes = 0;
+        if (j.field == STNTT_FIELD_GL64) {
+            if (j.log_n > 32)
+                return fail(ctx, STNTT_EUNSUPPORTED, "job " + std::to_string(i) + ": log_n > 32");
+            f = kFieldGL;
+        } else if (j.field == STNTT_FIELD_U32) {
+            int rc = check_u32_args(ctx, j.log_n, j.p, j.root);
+            if (rc)
+                return rc;
+            f = kFieldU32;
+        } else {
+            return fail(ctx, STNTT_EINVAL, "job " + std::to_string(i) + ": unknown field");
+        }
+        size_t scratch_need = 0;
+        if (j.log_n >= 4) {
+            const Plan *pl;
+            uint64_t root = j.root;
+            if (f == kFieldGL)
+                stntt_gl64_root(j.log_n, &root);
+            int rc = get_plan(ctx, f, j.log_n, f == kFieldGL ? 0 : j.p, root, (int)j.dir, &pl);
+            if (rc)
+                return rc;
+            passes = (uint32_t)pl->passes.size();
+            for (const PassDesc &d : pl->passes)
+                if (d.logL < 4)
+                    passes = 99;  // the persistent kernel's tiles are at least 16 long
+            if (passes == 2)
+                scratch_need = ((size_t)1 << j.log_n) * (f == kFieldGL ? 8 : 4);
+        }
+        if (j.log_n >= 4 && passes <= 2) {
+            by_field[f].push_back(&j);
+            scratch_total += scratch_need;
+        } else {
+            bt->fallback.push_back(j);
+        }
+    }
+    if (scratch_total) {
+        cudaError_t e = cudaMalloc(&bt->d_scratch, scratch_total);
+        if (e != cudaSuccess)
+            return fail(ctx, STNTT_ENOMEM, std::string("cudaMalloc(batch scratch): ") + cudaGetErrorString(e));
+        bt->scratch_bytes = scratch_total;
+    }
+    size_t cursor = 0;
+    for (int f = 0; f < 2; ++f) {
+        if (by_field[f].empty())
+            continue;
+        int rc = build_part(ctx, bt.get(), f, by_field[f], cursor);
+        if (rc) {
+            stntt_batch_destroy(bt.release());
+            return rc;
+        }
+    }
+    *out = bt.release();
+    return STNTT_OK;
+}
+
+int stntt_batch_launch(stntt_batch *b, stntt_stream stream) {
+    if (!b)
+        return STNTT_EINVAL;
+    stntt_ctx *ctx = b->ctx;
+    DeviceGuard g(ctx->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    for (BatchPart &P : b->parts) {
+        char *base = static_cast<char *>(P.d_buf);
+        cudaError_t e = cudaMemsetAsync(base + P.counters_off, 0, P.bytes - P.counters_off, s);
+        if (e == cudaSuccess)
+            e = P.field == kFieldGL
+                    ? batch_launch_gl64(base + P.args_off, base + P.items_off, P.nitems,
+                                        reinterpret_cast<unsigned int *>(base + P.counters_off), base + P.ctl_off,
+                                        P.smem, P.grid, b->spin_limit, s)
+                    : batch_launch_u32(base + P.args_off, base + P.items_off, P.nitems,
+                                       reinterpret_cast<unsigned int *>(base + P.counters_off), base + P.ctl_off,
+                                       P.smem, P.grid, b->spin_limit, s);
+        if (e != cudaSuccess)
+            return cuda_fail(ctx, e, "batch launch");
+    }
+    if (!b->fallback.empty())
+        return stntt_ntt_batch_per_call(ctx, b->fallback.data(), b->fallback.size(), stream);
+    return STNTT_OK;
+}
+
+int stntt_batch_status(stntt_batch *b) {
+    if (!b)
+        return STNTT_EINVAL;
+    DeviceGuard g(b->ctx->device);
+    for (BatchPart &P : b->parts) {
+        BatchCtlH c;
+        cudaError_t e = cudaMemcpy(&c, static_cast<char *>(P.d_buf) + P.ctl_off, sizeof(c), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess)
+            return cuda_fail(b->ctx, e, "batch status");
+        if (c.error)
+            return fail(b->ctx, STNTT_ETIMEOUT,
+                        std::to_string(c.timeouts) + " batch work item(s) gave up waiting for their first pass");
+    }
+    return STNTT_OK;
+}
+
+int stntt_batch_info(const stntt_batch *b, size_t *items, uint32_t *grid, size_t *fallback) {
+    if (!b)
+        return STNTT_EINVAL;
+    size_t it = 0;
+    uint32_t gr = 0;
+    for (const BatchPart &P : b->parts) {
+        it += P.nitems;
+        gr += P.grid;
+    }
+    if (items)
+        *items = it;
+    if (grid)
+        *grid = gr;
+    if (fallback)
+        *fallback = b->fallback.size();
+    return STNTT_OK;
+}
+
+int stntt_batch_destroy(stntt_batch *b) {
+    if (!b)
+        return STNTT_EINVAL;
+    DeviceGuard g(b->ctx->device);
+    cudaDeviceSynchronize();
+    for (BatchPart &P : b->parts)
+        if (P.d_buf)
+            cudaFree(P.d_buf);
+    if (b->d_scratch)
+        cudaFree(b->d_scratch);
+    delete b;
+    return STNTT_OK;
+}
+
+int stntt_ntt_batch(stntt_ctx *ctx, const stntt_job *jobs, size_t njobs, stntt_stream stream) {
+    stntt_batch *b = nullptr;
+    int rc = stntt_batch_create(ctx, jobs, njobs, &b);
+    if (rc)
+        return rc;
+    rc = stntt_batch_launch(b, stream);
+    if (!rc) {
+        cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+        rc = e == cudaSuccess ? stntt_batch_status(b) : cuda_fail(ctx, e, "batch execution");
+    }
+    stntt_batch_destroy(b);
+    return rc;
+}
+
+int stntt_selftest_wait_timeout(stntt_ctx *ctx, uint32_t spin_limit) {
+    if (!ctx || spin_limit == 0)
+        return STNTT_EINVAL;
+    DeviceGuard g(ctx->device);
+    stntt_batch b;
+    b.ctx = ctx;
+    b.spin_limit = spin_limit;
+    BatchPart P;
+    P.field = kFieldGL;
+    P.nitems = 1;
+    P.ncounters = 1;
+    P.smem = 0;
+    P.grid = 1;
+    const size_t asz = args_size(kFieldGL);
+    P.args_off = 0;
+    P.items_off = 256 * ((asz + 255) / 256);
+    P.ptr_off = P.items_off + 256;
+    P.counters_off = P.ptr_off + 256;
+    P.ctl_off = P.counters_off + 256;
+    P.bytes = P.ctl_off + 256;
+    cudaError_t e = cudaMalloc(&P.d_buf, P.bytes);
+    if (e != cudaSuccess)
+        return fail(ctx, STNTT_ENOMEM, "selftest allocation");
+    std::vector<unsigned char> host(P.bytes, 0);
+    // one item that waits for a job counter nothing increments
+    BatchItemH it{0u, 0u, 1u, ~0u, 0ull};
+    std::memcpy(host.data() + P.items_off, &it, sizeof(it));
+    int bps = 0;
+    e = cudaMemcpy(P.d_buf, host.data(), P.bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = batch_prepare_gl64(0, &bps);
+    if (e != cudaSuccess) {
+        cudaFree(P.d_buf);
+        return cuda_fail(ctx, e, "selftest setup");
+    }
+    b.parts.push_back(P);
+    int rc = stntt_batch_launch(&b, nullptr);
+    if (!rc) {
+        e = cudaStreamSynchronize(nullptr);
+        rc = e == cudaSuccess ? stntt_batch_status(&b) : cuda_fail(ctx, e, "selftest run");
+    }
+    cudaFree(P.d_buf);
+    b.parts.clear();
+    return rc;
 }
 
 }  // extern "C"

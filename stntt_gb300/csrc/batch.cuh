@@ -1,0 +1,91 @@
+// batch.cuh -- one persistent launch for many transforms of uneven sizes.
+//
+// The host turns a job list into CTA-sized work items (tiles of C columns or
+// rows of length L with C * L = 8192, so every item uses 512 threads):
+// single-pass jobs of one (size, direction) are packed C transforms per item,
+// two-pass jobs contribute their first-pass items and, later in the list,
+// their second-pass items. Blocks take items in list order from one atomic
+// counter. A second-pass item waits until its job's first-pass items have
+// signalled; those were claimed earlier by running blocks that wait on
+// nothing, so the wait always ends. Every wait is bounded: past `spin_limit`
+// polls the item is skipped, an error flag is set and the host reports
+// STNTT_ETIMEOUT.
+//
+// This extends the reference's uniform `batches` packing
+// (src/cuda/ntt/ntt_kernel.cuh:31-39: one n per launch, transforms laid along
+// blockDim.y) to mixed sizes, fields' parameters and directions.
+#pragma once
+#include "tile.cuh"
+
+namespace stntt {
+
+struct BatchItem {
+    uint32_t args;        // index of this item's TileArgs
+    uint32_t wait_job;    // job whose first pass must finish first, or ~0u
+    uint32_t wait_count;  // number of first-pass items of that job
+    uint32_t signal_job;  // job to signal when this item is done, or ~0u
+    uint64_t blk;         // CTA index within the item's pass
+};
+
+struct BatchCtl {
+    unsigned long long next;  // next item to take
+    unsigned int error;       // set when a bounded wait gave up
+    unsigned int timeouts;
+};
+
+constexpr int kBatchThreads = 512;  // C * L / 16 for every item
+
+template <class F>
+__global__ void __launch_bounds__(kBatchThreads, 2) batch_kernel(const TileArgs<F> *__restrict__ args,
+                                                              const BatchItem *__restrict__ items,
+                                                              unsigned long long nitems, unsigned int *counters,
+                                                              BatchCtl *ctl, unsigned int spin_limit) {
+    using T = typename F::T;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ TileArgs<F> sa;
+    __shared__ unsigned long long s_item;
+    __shared__ int s_ok;
+    T *sm = reinterpret_cast<T *>(smem_raw);
+    for (;;) {
+        if (threadIdx.x == 0)
+            s_item = atomicAdd(&ctl->next, 1ull);
+        __syncthreads();
+        const unsigned long long it = s_item;
+        if (it >= nitems)
+            break;
+        const BatchItem bi = items[it];
+        if (threadIdx.x == 0) {
+            int ok = 1;
+            if (bi.wait_job != ~0u) {
+                unsigned int spins = 0;
+                while (atomicAdd(&counters[bi.wait_job], 0u) < bi.wait_count) {
+                    if (++spins > spin_limit) {
+                        ok = 0;
+                        atomicExch(&ctl->error, 1u);
+                        atomicAdd(&ctl->timeouts, 1u);
+                        break;
+                    }
+                    __nanosleep(200);
+                }
+                __threadfence();
+            }
+            s_ok = ok;
+            sa = args[bi.args];
+        }
+        __syncthreads();
+        if (s_ok) {
+            switch (sa.logL & 3) {
+            case 0: tile_run<F, 16, 0>(sa, bi.blk, sm); break;
+            case 1: tile_run<F, 16, 1>(sa, bi.blk, sm); break;
+            case 2: tile_run<F, 16, 2>(sa, bi.blk, sm); break;
+            default: tile_run<F, 16, 3>(sa, bi.blk, sm); break;
+            }
+        }
+        __threadfence();  // this item's stores before the signal below
+        __syncthreads();
+        if (threadIdx.x == 0 && bi.signal_job != ~0u)
+            atomicAdd(&counters[bi.signal_job], 1u);
+    }
+}
+
+}  // namespace stntt

@@ -3,6 +3,7 @@
 #pragma once
 #include <cstring>
 
+#include "batch.cuh"
 #include "internal.h"
 #include "tile.cuh"
 
@@ -38,11 +39,9 @@ cudaError_t launch_tile_e(const PassDesc &d, const TileArgs<F> &a, uint64_t bloc
 }
 
 template <class F>
-cudaError_t launch_tile_t(const PassDesc &d, uint32_t p, const void *tables, const void *in, void *out,
-                          uint64_t batch, cudaStream_t s) {
+void fill_args(TileArgs<F> &a, const PassDesc &d, uint32_t p, const void *tables, const void *in, void *out) {
     using T = typename F::T;
     using TW = typename F::TW;
-    TileArgs<F> a;
     const TW *tab = static_cast<const TW *>(tables);
     a.in = static_cast<const T *>(in);
     a.out = static_cast<T *>(out);
@@ -65,6 +64,16 @@ cudaError_t launch_tile_t(const PassDesc &d, uint32_t p, const void *tables, con
     a.logN1 = d.logN1;
     a.logN2 = d.logN2;
     a.cs = d.cs;
+    a.in_ptrs = nullptr;
+    a.out_ptrs = nullptr;
+    a.total = 0;
+}
+
+template <class F>
+cudaError_t launch_tile_t(const PassDesc &d, uint32_t p, const void *tables, const void *in, void *out,
+                          uint64_t batch, cudaStream_t s) {
+    TileArgs<F> a;
+    fill_args<F>(a, d, p, tables, in, out);
     const uint64_t rows = batch << (d.logN - d.logL);
     a.total = rows;
     const uint64_t blocks = (rows + (1ull << d.logC) - 1) >> d.logC;
@@ -93,6 +102,43 @@ cudaError_t launch_tile_t(const PassDesc &d, uint32_t p, const void *tables, con
         }
     default: return cudaErrorInvalidValue;
     }
+}
+
+// ---- persistent batched launch (batch.cuh)
+template <class F>
+size_t batch_args_size_t() {
+    return sizeof(TileArgs<F>);
+}
+
+// One item descriptor for a pass over transforms whose data pointers are in
+// in_ptrs / out_ptrs (device arrays), `total` columns or rows in all.
+template <class F>
+void batch_args_fill_t(const PassDesc &d, uint32_t p, const void *tables, const unsigned long long *in_ptrs,
+                       const unsigned long long *out_ptrs, uint64_t total, void *dst) {
+    TileArgs<F> a;
+    fill_args<F>(a, d, p, tables, nullptr, nullptr);
+    a.in_ptrs = in_ptrs;
+    a.out_ptrs = out_ptrs;
+    a.total = total;
+    memcpy(dst, &a, sizeof(a));
+}
+
+template <class F>
+cudaError_t batch_prepare_t(size_t smem, int *blocks_per_sm) {
+    auto kern = batch_kernel<F>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e != cudaSuccess)
+        return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, kern, kBatchThreads, smem);
+}
+
+template <class F>
+cudaError_t batch_launch_t(const void *args, const void *items, unsigned long long nitems, unsigned int *counters,
+                           void *ctl, size_t smem, unsigned grid, unsigned spin_limit, cudaStream_t s) {
+    batch_kernel<F><<<grid, kBatchThreads, smem, s>>>(static_cast<const TileArgs<F> *>(args),
+                                                       static_cast<const BatchItem *>(items), nitems, counters,
+                                                       static_cast<BatchCtl *>(ctl), spin_limit);
+    return cudaGetLastError();
 }
 
 // out[i] = scale * base^i as twiddle entries

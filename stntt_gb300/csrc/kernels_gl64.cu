@@ -64,4 +64,15 @@ cudaError_t copy_scale_gl64(const void *in, void *out, size_t count, uint64_t sc
     return cudaGetLastError();
 }
 
+size_t batch_args_size_gl64() { return batch_args_size_t<FieldGL>(); }
+void batch_args_fill_gl64(const PassDesc &d, uint32_t p, const void *tables, const unsigned long long *in_ptrs,
+                         const unsigned long long *out_ptrs, uint64_t total, void *dst) {
+    batch_args_fill_t<FieldGL>(d, p, tables, in_ptrs, out_ptrs, total, dst);
+}
+cudaError_t batch_prepare_gl64(size_t smem, int *blocks_per_sm) { return batch_prepare_t<FieldGL>(smem, blocks_per_sm); }
+cudaError_t batch_launch_gl64(const void *args, const void *items, unsigned long long nitems, unsigned int *counters,
+                             void *ctl, size_t smem, unsigned grid, unsigned spin_limit, cudaStream_t s) {
+    return batch_launch_t<FieldGL>(args, items, nitems, counters, ctl, smem, grid, spin_limit, s);
+}
+
 }  // namespace stntt

@@ -114,4 +114,15 @@ cudaError_t copy_scale_u32(const void *in, void *out, size_t count, uint64_t sca
     return cudaGetLastError();
 }
 
+size_t batch_args_size_u32() { return batch_args_size_t<FieldU32>(); }
+void batch_args_fill_u32(const PassDesc &d, uint32_t p, const void *tables, const unsigned long long *in_ptrs,
+                         const unsigned long long *out_ptrs, uint64_t total, void *dst) {
+    batch_args_fill_t<FieldU32>(d, p, tables, in_ptrs, out_ptrs, total, dst);
+}
+cudaError_t batch_prepare_u32(size_t smem, int *blocks_per_sm) { return batch_prepare_t<FieldU32>(smem, blocks_per_sm); }
+cudaError_t batch_launch_u32(const void *args, const void *items, unsigned long long nitems, unsigned int *counters,
+                             void *ctl, size_t smem, unsigned grid, unsigned spin_limit, cudaStream_t s) {
+    return batch_launch_t<FieldU32>(args, items, nitems, counters, ctl, smem, grid, spin_limit, s);
+}
+
 }  // namespace stntt

@@ -47,6 +47,10 @@ struct TileArgs {
     uint32_t logN1, logN2;  // ROW: rows r map to input row ((r mod n1) * n2 + r / n1)
     uint32_t cs;            // shared-memory column stride, elements
     uint64_t total;         // columns (COL) or rows (ROW) over the whole batch
+    // Optional per-transform base pointers (batched jobs): transform b reads
+    // from in_ptrs[b] and writes to out_ptrs[b] instead of in/out + b*n.
+    const unsigned long long *in_ptrs;
+    const unsigned long long *out_ptrs;
 };
 
 template <class F>
@@ -87,14 +91,18 @@ __device__ __forceinline__ void dft_reg(const F &f, typename F::T *x, const type
     }
 }
 
+template <class T>
 struct Geo {
-    uint64_t ibase, istride, obase, ostride, col;
+    const T *src;  // element j of this column/row: src[j * istride]
+    T *dst;        // element k: dst[k * ostride]
+    uint64_t istride, ostride, col;
     bool valid;  // false for the padding rows of a partial last CTA
 };
 
 template <class F, int E, int LOGR, bool first, bool last>
 __device__ __forceinline__ void tile_step(const TileArgs<F> &a, const F &f, typename F::T (&x)[E],
-                                          typename F::T *sm, uint32_t c, uint32_t u, uint32_t logp, const Geo &g) {
+                                          typename F::T *sm, uint32_t c, uint32_t u, uint32_t logp,
+                                          const Geo<typename F::T> &g) {
     using T = typename F::T;
     constexpr int R = 1 << LOGR, ITEMS = E / R;
     const uint32_t L = 1u << a.logL, U = L / E, T_ = L >> LOGR;
@@ -109,7 +117,7 @@ __device__ __forceinline__ void tile_step(const TileArgs<F> &a, const F &f, type
         for (int r = 0; r < R; ++r) {
             const uint32_t idx = t + r * T_;
             if constexpr (first)
-                x[m * R + r] = g.valid ? a.in[g.ibase + (uint64_t)idx * g.istride] : T(0);
+                x[m * R + r] = g.valid ? g.src[(uint64_t)idx * g.istride] : T(0);
             else
                 x[m * R + r] = col_sm[Pad<F>::at(idx)];
         }
@@ -149,7 +157,7 @@ __device__ __forceinline__ void tile_step(const TileArgs<F> &a, const F &f, type
                     v = f.mul_tw(v, a.scale);
                 }
                 if (g.valid)
-                    a.out[g.obase + (uint64_t)pos * g.ostride] = v;
+                    g.dst[(uint64_t)pos * g.ostride] = v;
             } else {
                 col_sm[Pad<F>::at(pos)] = v;
             }
@@ -159,11 +167,12 @@ __device__ __forceinline__ void tile_step(const TileArgs<F> &a, const F &f, type
         __syncthreads();
 }
 
+// One CTA's worth of work: C columns (COL) or rows (ROW) with global index
+// blk * C + c over the batch. Used by tile_kernel (blk = blockIdx.x) and by
+// the persistent batched kernel (blk from its work list).
 template <class F, int E, int TAIL>
-__global__ void __launch_bounds__(E >= 32 ? 512 : 1024) tile_kernel(const TileArgs<F> a) {
+__device__ __forceinline__ void tile_run(const TileArgs<F> &a, uint64_t blk, typename F::T *sm) {
     using T = typename F::T;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T *sm = reinterpret_cast<T *>(smem_raw);
     F f;
     f.p = a.p;
 
@@ -178,24 +187,31 @@ __global__ void __launch_bounds__(E >= 32 ? 512 : 1024) tile_kernel(const TileAr
         c = threadIdx.x & (C - 1);
         u = threadIdx.x >> a.logC;
     }
-    const uint64_t gi = ((uint64_t)blockIdx.x << a.logC) + c;
-    const uint32_t logPer = a.logN - a.logL;
+    // global column / row index over the whole batch
+    const uint64_t gi = (blk << a.logC) + c;
+    const uint32_t logPer = a.logN - a.logL;  // columns (rows) per transform
     const uint64_t b = gi >> logPer;
     const uint64_t rem = gi & ((1ull << logPer) - 1);
-    const uint64_t tbase = b << a.logN;
-    Geo g;
+    Geo<T> g;
     g.valid = gi < a.total;
+    const T *ibase = a.in + (b << a.logN);
+    T *obase = a.out + (b << a.logN);
+    if (a.in_ptrs && g.valid) {
+        ibase = reinterpret_cast<const T *>(a.in_ptrs[b]);
+        obase = reinterpret_cast<T *>(a.out_ptrs[b]);
+    }
     if (a.mode == kModeCol) {
         const uint64_t q = rem >> a.logS;
         g.col = rem & ((1ull << a.logS) - 1);
-        g.ibase = g.obase = tbase + (q << a.logM) + g.col;
+        g.src = ibase + (q << a.logM) + g.col;
+        g.dst = obase + (q << a.logM) + g.col;
         g.istride = g.ostride = 1ull << a.logS;
     } else {
         const uint64_t inrow = ((rem & ((1ull << a.logN1) - 1)) << a.logN2) + (rem >> a.logN1);
         g.col = 0;
-        g.ibase = tbase + (inrow << a.logL);
+        g.src = ibase + (inrow << a.logL);
         g.istride = 1;
-        g.obase = tbase + rem;
+        g.dst = obase + rem;
         g.ostride = 1ull << logPer;
     }
 
@@ -225,6 +241,12 @@ __global__ void __launch_bounds__(E >= 32 ? 512 : 1024) tile_kernel(const TileAr
         }
         tile_step<F, E, 4, false, true>(a, f, x, sm, c, u, logp, g);
     }
+}
+
+template <class F, int E, int TAIL>
+__global__ void __launch_bounds__(E >= 32 ? 512 : 1024) tile_kernel(const TileArgs<F> a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    tile_run<F, E, TAIL>(a, blockIdx.x, reinterpret_cast<typename F::T *>(smem_raw));
 }
 
 }  // namespace stntt

@@ -1,0 +1,112 @@
+"""Uneven batches in one persistent launch (stntt_ntt_batch / stntt_batch_*).
+
+Every job is checked bit for bit against the CPU oracle and against one
+launch sequence per job; a reusable batch is replayed from a CUDA graph; a
+bounded device-side wait is made to run out and must report STNTT_ETIMEOUT.
+"""
+
+import numpy as np
+import pytest
+
+import oracle as O
+import stntt_gb300 as st
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def _make_jobs(seed, n_jobs, lo, hi, fields=("gl64", "u32"), extra=()):
+    rng = np.random.default_rng(seed)
+    jobs, bufs, inputs, meta = [], [], [], []
+    sizes = list(rng.integers(lo, hi + 1, n_jobs)) + list(extra)
+    for i, lg in enumerate(sizes):
+        lg = int(lg)
+        inv = i % 2
+        field = fields[i % len(fields)]
+        if field == "u32":
+            p, root = st.params_u32(lg)
+            x = O.uniform_u32(seed * 10000 + i, p, 1 << lg)
+            d = torch.from_numpy(x.view(np.int32).copy()).cuda()
+            jobs.append(st.Job(st.FIELD_U32, lg, inv, p, root, 0, d.data_ptr()))
+            meta.append(("u32", lg, inv, p, root))
+        else:
+            x = O.uniform_u64(seed * 10000 + i, 1 << lg)
+            d = torch.from_numpy(x.view(np.int64).copy()).cuda()
+            jobs.append(st.Job(st.FIELD_GL64, lg, inv, 0, 0, 0, d.data_ptr()))
+            meta.append(("gl64", lg, inv, 0, 0))
+        bufs.append(d)
+        inputs.append(x)
+    return jobs, bufs, inputs, meta
+
+
+def _expected(x, m):
+    field, lg, inv, p, root = m
+    if field == "u32":
+        return O.ntt_u32(x, root, p, inverse=bool(inv))
+    return O.ntt_gl64(x, inverse=bool(inv))
+
+
+def _host(d):
+    a = d.cpu().numpy()
+    return a.view(np.uint32) if d.dtype == torch.int32 else a.view(np.uint64)
+
+
+def test_batch_matches_oracle_and_per_call(ctx):
+    # mixed fields, directions and sizes, incl. tiny (< 2^4) and three-pass (2^25) jobs
+    jobs, bufs, inputs, meta = _make_jobs(3, 120, 4, 18, extra=(0, 1, 2, 3, 25))
+    ref_bufs = [b.clone() for b in bufs]
+    ctx.ntt_batch(jobs)
+    torch.cuda.synchronize()
+    for b, x, m in zip(bufs, inputs, meta):
+        assert np.array_equal(_host(b), _expected(x, m)), m
+    # per-call path on the same inputs gives the same bits
+    jobs2 = [st.Job(j.field, j.log_n, j.dir, j.p, j.root, 0, rb.data_ptr()) for j, rb in zip(jobs, ref_bufs)]
+    ctx.ntt_batch(jobs2, per_call=True)
+    torch.cuda.synchronize()
+    for b, rb in zip(bufs, ref_bufs):
+        assert torch.equal(b, rb)
+
+
+def test_batch_reference_mix_shape(ctx):
+    """The batched configuration's shape: Goldilocks, log2 n in [10, 18], half
+    forward and half inverse (a smaller count of jobs)."""
+    jobs, bufs, inputs, meta = _make_jobs(11, 256, 10, 18, fields=("gl64",))
+    b = ctx.batch_create(jobs)
+    info = b.info()
+    assert info["fallback_jobs"] == 0 and info["items"] > 0
+    b.launch()
+    torch.cuda.synchronize()
+    assert b.status() == 0
+    for d, x, m in zip(bufs, inputs, meta):
+        assert np.array_equal(_host(d), _expected(x, m)), m
+    b.close()
+
+
+def test_batch_graph_replay(ctx):
+    jobs, bufs, inputs, meta = _make_jobs(21, 40, 6, 17)
+    b = ctx.batch_create(jobs)
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        b.launch(stream=s)
+    # capture does not run the work; each replay transforms in place once
+    for rep in range(2):
+        for d, x in zip(bufs, inputs):
+            d.copy_(torch.from_numpy(x.view(np.int32 if d.dtype == torch.int32 else np.int64).copy()))
+        torch.cuda.synchronize()
+        g.replay()
+        torch.cuda.synchronize()
+        assert b.status() == 0
+        for d, x, m in zip(bufs, inputs, meta):
+            assert np.array_equal(_host(d), _expected(x, m)), (rep, m)
+    b.close()
+
+
+def test_bounded_wait_reports_timeout(ctx):
+    assert ctx.selftest_wait_timeout(20000) == 4  # STNTT_ETIMEOUT
+    # the context stays usable afterwards
+    x = O.uniform_u64(5, 1 << 12)
+    d = torch.from_numpy(x.view(np.int64).copy()).cuda()
+    ctx.ntt_gl64(d, 12)
+    torch.cuda.synchronize()
+    assert np.array_equal(_host(d), O.ntt_gl64(x))
