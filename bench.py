@@ -39,7 +39,8 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 WORKLOADS = {
-    # name: (field, log_n)
+    # name: (field, log_n); "batch" = the uneven mix below
+    "gl64_batch_mix": ("gl64", "batch"),
     "gl64_2^24_fwd+inv": ("gl64", 24),
     "gl64_2^20_fwd+inv": ("gl64", 20),
     "u32_2^26_fwd+inv": ("u32", 26),
@@ -146,6 +147,10 @@ def run_reference(args):
     import oracle as O
 
     field, lg = WORKLOADS[args.workload]
+    if lg == "batch":
+        print(json.dumps({"impl": "reference", "unavailable": "the CPU reference arm covers the single-transform "
+                          "workloads; run it with the default workload"}), flush=True)
+        return
     n = 1 << lg
     threads = max(1, min(O.cpu_count(), 16))
     kind = "port"
@@ -208,10 +213,110 @@ def cpu_baseline(field: str, lg: int):
                       "the reference Stockham loop (src/ntt/ntt_cpu.cpp:46-85)"}
 
 
+# --------------------------------------------------------------------------- batched mix
+MIX_JOBS, MIX_LO, MIX_HI, MIX_SEED = 4096, 10, 18, 0x57170001 + 3
+
+
+def mix_sizes():
+    """log2 n of each job: uniform in [10, 18] from a fixed seed; job i is
+    forward for even i and inverse for odd i."""
+    rng = np.random.default_rng(MIX_SEED)
+    return [int(v) for v in rng.integers(MIX_LO, MIX_HI + 1, MIX_JOBS)]
+
+
+def run_batch_mix(args):
+    rank, world, local = dist_env()
+    import torch
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+    import stntt_gb300 as st
+
+    sizes = mix_sizes()
+    total = sum(1 << s for s in sizes)
+    data = torch.empty(total, dtype=torch.int64, device=dev)
+    st.fill_uniform_gl64(data, 77 + rank)
+    jobs, off = [], 0
+    for i, s in enumerate(sizes):
+        jobs.append(st.Job(st.FIELD_GL64, s, i % 2, 0, 0, 0, data.data_ptr() + 8 * off))
+        off += 1 << s
+    ctx = st.Context(local)
+    b = ctx.batch_create(jobs)
+    info = b.info()
+    stream = torch.cuda.Stream(device=dev)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=stream):
+        b.launch(stream=stream)
+    for _ in range(args.warmup):
+        g.replay()
+    torch.cuda.synchronize()
+    ok = b.status() == 0
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.25)
+    if world > 1:
+        torch.distributed.barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(args.steps):
+        g.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = sampler.stop()
+    ok = ok and b.status() == 0
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * total / (ms / 1e3) / 1e9
+    # one launch sequence per transform (the comparison), plain launches
+    s2 = torch.cuda.current_stream()
+    ctx.ntt_batch(jobs, per_call=True, stream=s2)
+    torch.cuda.synchronize()
+    k = max(1, min(args.steps, 5))
+    e0.record()
+    for _ in range(k):
+        ctx.ntt_batch(jobs, per_call=True, stream=s2)
+    e1.record()
+    torch.cuda.synchronize()
+    per_ms = e0.elapsed_time(e1) / k
+    hbm, hbm_kind = peaks()
+    b_alg = sum((2 if s <= 13 else 4) * (1 << s) * 8 for s in sizes)
+    achieved = b_alg / (ms / 1e3) / 1e9
+    if rank == 0:
+        print(json.dumps({
+            "metric": "NTT Gelem/s (uneven batch: 4096 Goldilocks transforms, log2 n in [10,18])",
+            "value": value, "unit": "Gelem/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic (splitmix64 uniform residues)",
+            "config": {"workload": "gl64_batch_mix", "jobs": MIX_JOBS, "log_n_range": [MIX_LO, MIX_HI],
+                       "seed": MIX_SEED, "elements": total, "directions": "alternating forward / inverse",
+                       "launch": "one persistent launch replayed from a CUDA graph", **info},
+            "per_call": {"value": world * total / (per_ms / 1e3) / 1e9, "ms_per_step": per_ms,
+                         "launch": "one launch sequence per transform (stntt_ntt_batch_per_call)"},
+            "speedup_vs_per_call": per_ms / ms,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "peak_kind": hbm_kind, "b_alg_per_step": b_alg},
+            "clocks": clocks, "gpu_launches": args.steps, "status_ok": ok}), flush=True)
+    b.close()
+    ctx.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if WORKLOADS[args.workload][1] == "batch":
+        run_batch_mix(args)
         return
     rank, world, local = dist_env()
     import torch
