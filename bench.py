@@ -41,6 +41,7 @@ sys.path.insert(0, str(ROOT))
 WORKLOADS = {
     # name: (field, log_n); "batch" = the uneven mix below
     "gl64_batch_mix": ("gl64", "batch"),
+    "serve_mix": ("mixed", "serve"),
     "gl64_2^24_fwd+inv": ("gl64", 24),
     "gl64_2^20_fwd+inv": ("gl64", 20),
     "u32_2^26_fwd+inv": ("u32", 26),
@@ -147,7 +148,7 @@ def run_reference(args):
     import oracle as O
 
     field, lg = WORKLOADS[args.workload]
-    if lg == "batch":
+    if lg in ("batch", "serve"):
         print(json.dumps({"impl": "reference", "unavailable": "the CPU reference arm covers the single-transform "
                           "workloads; run it with the default workload"}), flush=True)
         return
@@ -310,10 +311,101 @@ def run_batch_mix(args):
     ctx.close()
 
 
+# --------------------------------------------------------------------------- serving loop
+SERVE_RATE, SERVE_LO, SERVE_HI, SERVE_SEED = 20000.0, 12, 22, 0x57170001 + 4
+
+
+def run_serve_mix(args):
+    """Seeded Poisson stream (mean 20k requests/s): 70% single NTTs, 30%
+    cyclic polynomial products of two polynomials of degree < n/2, n = 2^k with
+    k uniform in [12, 22], 50/50 32-bit prime / Goldilocks. `--steps` scales
+    the number of requests (steps * 1000)."""
+    import torch
+    import stntt_gb300 as st
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    count = max(1000, args.steps * 1000)
+    rng = np.random.default_rng(SERVE_SEED)
+    arrivals = np.cumsum(rng.exponential(1.0 / SERVE_RATE, count))
+    kinds = rng.random(count) < 0.3
+    logs = rng.integers(SERVE_LO, SERVE_HI + 1, count)
+    gls = rng.integers(0, 2, count).astype(bool)
+    dirs = rng.integers(0, 2, count)
+    # operand pool: one pinned (a, b, out) triple per (field, size); inputs read-only
+    pool = {}
+    for lg in range(SERVE_LO, SERVE_HI + 1):
+        n = 1 << lg
+        for gl in (False, True):
+            dt = torch.int64 if gl else torch.int32
+            a, b, o = (torch.zeros(n, dtype=dt, pin_memory=True) for _ in range(3))
+            if gl:
+                a.numpy().view(np.uint64)[:] = st.uniform_gl64_host(lg, n)
+                b.numpy().view(np.uint64)[: n // 2] = st.uniform_gl64_host(100 + lg, n // 2)
+                a2 = a.clone().pin_memory()
+                a2.numpy()[n // 2:] = 0
+            else:
+                p, _ = st.params_u32(lg)
+                a.numpy().view(np.uint32)[:] = st.uniform_u32_host(lg, p, n)
+                b.numpy().view(np.uint32)[: n // 2] = st.uniform_u32_host(100 + lg, p, n // 2)
+                a2 = a.clone().pin_memory()
+                a2.numpy()[n // 2:] = 0
+            pool[(gl, lg)] = (a, a2, b, o)
+    ctx = st.Context(local)
+    sv = st.Server(ctx, streams=16, max_log_n=SERVE_HI, prewarm=(SERVE_LO, SERVE_HI))
+    reqs = []
+    for i in range(count):
+        lg, gl = int(logs[i]), bool(gls[i])
+        a, a2, b, o = pool[(gl, lg)]
+        p, root = (0, 0) if gl else st.params_u32(lg)
+        if kinds[i]:
+            reqs.append(st.Request(st.REQ_POLYMUL, st.FIELD_GL64 if gl else st.FIELD_U32, lg, 0, p, root, i,
+                                   a2.data_ptr(), b.data_ptr(), o.data_ptr()))
+        else:
+            reqs.append(st.Request(st.REQ_NTT, st.FIELD_GL64 if gl else st.FIELD_U32, lg, int(dirs[i]), p, root, i,
+                                   a.data_ptr(), 0, o.data_ptr()))
+    # warm-up: the first few requests, run to completion
+    sv.run_trace(reqs[: min(200, count)], [0.0] * min(200, count))
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.25)
+    t0 = time.perf_counter()
+    comps = sv.run_trace(reqs, list(arrivals))
+    wall = time.perf_counter() - t0
+    clocks = sampler.stop()
+    ok = all(c.status == 0 for c in comps)
+    lat = np.array([c.done_s - c.submit_s for c in comps]) * 1e3
+    qwait = np.array([c.start_s - c.submit_s for c in comps]) * 1e3
+    span = max(c.done_s for c in comps) - min(c.submit_s for c in comps)
+    elems = float(sum((3 if kinds[i] else 1) * (1 << int(logs[i])) for i in range(count)))
+    stats = sv.stats()
+    sv.close()
+    ctx.close()
+    if rank == 0:
+        print(json.dumps({
+            "metric": "serving: p50/p99 request latency (ms) and throughput at 20k requests/s offered",
+            "value": float(np.percentile(lat, 99)), "unit": "ms (p99 latency)", "higher_is_better": False,
+            "n_gpus": world, "steps": args.steps, "warmup": 200, "ms_per_step": None, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u32+u64", "data": "synthetic (splitmix64 residues, seeded Poisson trace)",
+            "config": {"workload": "serve_mix", "requests": count, "rate_per_s": SERVE_RATE,
+                       "log_n_range": [SERVE_LO, SERVE_HI], "polymul_fraction": 0.3, "fields": "50/50",
+                       "streams": 16, "seed": SERVE_SEED},
+            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p90": float(np.percentile(lat, 90)),
+                           "p99": float(np.percentile(lat, 99)), "max": float(lat.max()),
+                           "queue_p50": float(np.percentile(qwait, 50)),
+                           "queue_p99": float(np.percentile(qwait, 99))},
+            "throughput": {"requests_per_s": count / span, "offered_per_s": SERVE_RATE,
+                           "transform_gelem_per_s": elems / span / 1e9, "span_s": span, "wall_s": wall},
+            "server": stats, "clocks": clocks, "status_ok": ok}), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if WORKLOADS[args.workload][1] == "serve":
+        run_serve_mix(args)
         return
     if WORKLOADS[args.workload][1] == "batch":
         run_batch_mix(args)

@@ -186,6 +186,54 @@ int stntt_pointwise_mul_u32(const uint32_t *d_a, const uint32_t *d_b, uint32_t *
 int stntt_pointwise_mul_gl64(const uint64_t *d_a, const uint64_t *d_b, uint64_t *d_out, size_t count,
                              stntt_stream stream);
 
+/* ---- serving loop ------------------------------------------------------------------ */
+/* A request loop on one GPU (no counterpart in the reference; it composes
+ * nttStockham and pwcNtt, src/ntt/ntt_cpu.cpp:46-90,167-174). A scheduler
+ * thread admits requests in arrival order as soon as a stream slot is free and
+ * the server's device arena can hold their operands, runs each on its own
+ * stream (H2D, kernels, D2H) so requests overlap on the device, and records
+ * host timestamps. Host buffers should be pinned and must stay valid until the
+ * request completes. */
+#define STNTT_REQ_NTT 0u
+#define STNTT_REQ_POLYMUL 1u /* cyclic product of in_a and in_b, length 2^log_n */
+typedef struct stntt_request {
+    uint32_t kind, field, log_n, dir; /* dir: STNTT_REQ_NTT only */
+    uint32_t p, root;                 /* STNTT_FIELD_U32 only */
+    uint64_t id;                      /* echoed in the completion */
+    const void *in_a, *in_b;          /* host operands (in_b: polymul) */
+    void *out;                        /* host result, 2^log_n elements */
+} stntt_request;
+typedef struct stntt_completion {
+    uint64_t id;
+    int32_t status; /* STNTT_OK, or why the request failed */
+    uint32_t reserved;
+    double submit_s, start_s, done_s; /* stntt_clock_s() at submit, admission, completion */
+} stntt_completion;
+typedef struct stntt_server_config {
+    uint32_t streams;      /* request slots (CUDA streams); 0 = 16 */
+    uint32_t max_log_n;    /* largest request; per-slot workspaces are sized for it; 0 = 22 */
+    uint64_t arena_bytes;  /* device memory for operands; 0 = a quarter of free HBM, at most 8 GiB */
+    uint32_t prewarm_min_log_n, prewarm_max_log_n; /* build twiddle tables for this range at start */
+} stntt_server_config;
+typedef struct stntt_server_stats {
+    uint64_t submitted, admitted, completed, failed, rejected;
+    uint64_t peak_inflight, arena_bytes, peak_arena_used;
+} stntt_server_stats;
+typedef struct stntt_server stntt_server;
+double stntt_clock_s(void);
+int stntt_server_create(stntt_ctx *ctx, const stntt_server_config *cfg, stntt_server **out);
+int stntt_server_submit(stntt_server *sv, const stntt_request *req);
+/* submit with an explicit arrival time (stntt_clock_s units) for latency accounting */
+int stntt_server_submit_at(stntt_server *sv, const stntt_request *req, double t_submit);
+int stntt_server_poll(stntt_server *sv, stntt_completion *out, size_t max, size_t *got);
+int stntt_server_wait_idle(stntt_server *sv, double timeout_s);
+int stntt_server_stats_get(stntt_server *sv, stntt_server_stats *out);
+/* Native load driver: submits reqs[i] (whose id must be i) at arrival_s[i]
+ * seconds after the start, waits for all, writes completion i to out[i]. */
+int stntt_server_run_trace(stntt_server *sv, const stntt_request *reqs, const double *arrival_s, size_t n,
+                           double timeout_s, stntt_completion *out);
+int stntt_server_destroy(stntt_server *sv);
+
 /* ---- allocation-free variant ------------------------------------------------------ */
 /* No counterpart in the reference. For callers that cannot call cudaMalloc
  * (a memory pool that already owns HBM, a host runtime that manages device

@@ -53,6 +53,31 @@ class Job(C.Structure):
                 ("root", C.c_uint32), ("reserved", C.c_uint32), ("data", C.c_void_p)]
 
 
+class Request(C.Structure):
+    """``stntt_request`` (serving loop)."""
+
+    _fields_ = [("kind", C.c_uint32), ("field", C.c_uint32), ("log_n", C.c_uint32), ("dir", C.c_uint32),
+                ("p", C.c_uint32), ("root", C.c_uint32), ("id", C.c_uint64), ("in_a", C.c_void_p),
+                ("in_b", C.c_void_p), ("out", C.c_void_p)]
+
+
+class Completion(C.Structure):
+    _fields_ = [("id", C.c_uint64), ("status", C.c_int32), ("reserved", C.c_uint32), ("submit_s", C.c_double),
+                ("start_s", C.c_double), ("done_s", C.c_double)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("streams", C.c_uint32), ("max_log_n", C.c_uint32), ("arena_bytes", C.c_uint64),
+                ("prewarm_min_log_n", C.c_uint32), ("prewarm_max_log_n", C.c_uint32)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(k, C.c_uint64) for k in ("submitted", "admitted", "completed", "failed", "rejected",
+                                          "peak_inflight", "arena_bytes", "peak_arena_used")]
+
+
+REQ_NTT, REQ_POLYMUL = 0, 1
+
 _LIB = None
 _vp, _u32, _u64, _i32, _sz, _int = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int32, C.c_size_t, C.c_int
 
@@ -93,6 +118,16 @@ _SIGS = {
     "stntt_batch_info": (_int, [_vp, C.POINTER(_sz), C.POINTER(_u32), C.POINTER(_sz)]),
     "stntt_batch_destroy": (_int, [_vp]),
     "stntt_selftest_wait_timeout": (_int, [_vp, _u32]),
+    "stntt_clock_s": (C.c_double, []),
+    "stntt_server_create": (_int, [_vp, C.POINTER(ServerConfig), C.POINTER(_vp)]),
+    "stntt_server_submit": (_int, [_vp, C.POINTER(Request)]),
+    "stntt_server_submit_at": (_int, [_vp, C.POINTER(Request), C.c_double]),
+    "stntt_server_poll": (_int, [_vp, C.POINTER(Completion), _sz, C.POINTER(_sz)]),
+    "stntt_server_wait_idle": (_int, [_vp, C.c_double]),
+    "stntt_server_stats_get": (_int, [_vp, C.POINTER(ServerStats)]),
+    "stntt_server_run_trace": (_int, [_vp, C.POINTER(Request), C.POINTER(C.c_double), _sz, C.c_double,
+                                      C.POINTER(Completion)]),
+    "stntt_server_destroy": (_int, [_vp]),
 }
 
 
@@ -332,6 +367,55 @@ class Batch:
     def close(self) -> None:
         if self._h:
             lib().stntt_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):  # pragma: no cover
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """A ``stntt_server``: the request loop (see include/stntt.h)."""
+
+    def __init__(self, ctx: Context, streams: int = 16, max_log_n: int = 22, arena_bytes: int = 0,
+                 prewarm: tuple[int, int] | None = None):
+        cfg = ServerConfig(streams, max_log_n, arena_bytes, *(prewarm or (0, 0)))
+        h = _vp()
+        _check(lib().stntt_server_create(ctx.handle, C.byref(cfg), C.byref(h)), ctx.handle)
+        self.ctx, self._h = ctx, h.value
+
+    def submit(self, req: Request) -> int:
+        return lib().stntt_server_submit(self._h, C.byref(req))
+
+    def wait_idle(self, timeout_s: float = 60.0) -> int:
+        return lib().stntt_server_wait_idle(self._h, timeout_s)
+
+    def poll(self, max_items: int = 4096) -> list:
+        buf = (Completion * max_items)()
+        got = _sz()
+        _check(lib().stntt_server_poll(self._h, buf, max_items, C.byref(got)))
+        return [buf[i] for i in range(got.value)]
+
+    def run_trace(self, reqs: Sequence[Request], arrivals_s: Sequence[float], timeout_s: float = 120.0):
+        n = len(reqs)
+        r = (Request * n)(*reqs)
+        a = (C.c_double * n)(*arrivals_s)
+        out = (Completion * n)()
+        rc = lib().stntt_server_run_trace(self._h, r, a, n, timeout_s, out)
+        if rc not in (0,):
+            raise StnttError(rc, "run_trace")
+        return out
+
+    def stats(self) -> dict:
+        s = ServerStats()
+        _check(lib().stntt_server_stats_get(self._h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in ServerStats._fields_}
+
+    def close(self) -> None:
+        if self._h:
+            lib().stntt_server_destroy(self._h)
             self._h = None
 
     def __del__(self):  # pragma: no cover

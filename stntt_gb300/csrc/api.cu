@@ -22,6 +22,7 @@
 
 #include "../../include/stntt.h"
 #include "internal.h"
+#include "ctx_internal.h"
 
 namespace stntt {
 
@@ -138,7 +139,7 @@ using namespace stntt;
 // ---------------------------------------------------------------------------
 // context
 // ---------------------------------------------------------------------------
-namespace {
+namespace sd {
 
 struct PlanKey {
     int field;
@@ -168,7 +169,8 @@ struct PlanSpec {
     std::vector<uint32_t> logs, elems, cols;
 };
 
-}  // namespace
+}  // namespace sd
+using namespace sd;
 
 struct stntt_ctx {
     int device = 0;
@@ -186,7 +188,7 @@ struct stntt_ctx {
     size_t mem = 0;
 };
 
-namespace {
+namespace sd {
 
 int fail(stntt_ctx *ctx, int status, const std::string &msg) {
     if (ctx) {
@@ -573,7 +575,21 @@ int host_stage(stntt_ctx *ctx, size_t bytes, void **ptr) {
     return STNTT_OK;
 }
 
-}  // namespace
+int ctx_device(const stntt_ctx *ctx) { return ctx->device; }
+
+void release_workspace(stntt_ctx *ctx, cudaStream_t s) {
+    std::lock_guard<std::mutex> g(ctx->mu);
+    auto it = ctx->workspaces.find(s);
+    if (it == ctx->workspaces.end())
+        return;
+    cudaStreamSynchronize(s);
+    if (it->second.ptr)
+        cudaFree(it->second.ptr);
+    ctx->mem -= it->second.bytes;
+    ctx->workspaces.erase(it);
+}
+
+}  // namespace sd
 
 // ===========================================================================
 // C ABI
@@ -1032,7 +1048,9 @@ int stntt_pointwise_mul_gl64(const uint64_t *d_a, const uint64_t *d_b, uint64_t 
                                                                                                      : STNTT_ECUDA;
 }
 
-static int polymul_impl(stntt_ctx *ctx, int field, const void *a, const void *b, void *out, uint32_t log_n,
+}  // extern "C"
+namespace sd {
+int polymul_impl(stntt_ctx *ctx, int field, const void *a, const void *b, void *out, uint32_t log_n,
                         uint32_t p, uint64_t root, cudaStream_t s) {
     const size_t esz = field == kFieldGL ? 8 : 4;
     const size_t bytes = ((size_t)1 << log_n) * esz;
@@ -1058,6 +1076,8 @@ static int polymul_impl(stntt_ctx *ctx, int field, const void *a, const void *b,
         return cuda_fail(ctx, e, "pointwise launch");
     return run_plan(ctx, *inv, out, out, 1, s);
 }
+}  // namespace sd
+extern "C" {
 
 int stntt_polymul_u32(stntt_ctx *ctx, const uint32_t *d_a, const uint32_t *d_b, uint32_t *d_out, uint32_t log_n,
                       uint32_t p, uint32_t root, stntt_stream stream) {

@@ -1,0 +1,30 @@
+// ctx_internal.h -- context services shared by the C-ABI translation units
+// (api.cu defines them; serve.cu uses them). Not installed.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+#include "../../include/stntt.h"
+
+namespace sd {
+
+struct Plan;
+
+// Twiddle tables and pass list for one transform (built and cached on first use).
+int get_plan(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t p, uint64_t root, int dir, const Plan **out);
+// Run a plan: first pass reads `in`, last pass writes `out`, on stream s.
+int run_plan(stntt_ctx *ctx, const Plan &pl, const void *in, void *out, uint64_t batch, cudaStream_t s);
+// Per-stream scratch of at least `bytes` (grows with a synchronising cudaMalloc).
+int get_workspace(stntt_ctx *ctx, cudaStream_t s, size_t bytes, void **ptr);
+// Free the workspace of a stream that is about to be destroyed.
+void release_workspace(stntt_ctx *ctx, cudaStream_t s);
+// Cyclic product of two length-2^log_n operands (device pointers) on stream s.
+int polymul_impl(stntt_ctx *ctx, int field, const void *a, const void *b, void *out, uint32_t log_n, uint32_t p,
+                 uint64_t root, cudaStream_t s);
+int check_u32_args(stntt_ctx *ctx, uint32_t log_n, uint32_t p, uint32_t root);
+int fail(stntt_ctx *ctx, int status, const std::string &msg);
+int ctx_device(const stntt_ctx *ctx);
+
+}  // namespace sd
