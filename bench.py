@@ -489,6 +489,14 @@ def main():
     launch_ms = (float(np.mean(t_fwd)) + float(np.mean(t_inv))) / 2 / passes
     bytes_per_launch = 2 * n * esz
     achieved = bytes_per_launch / (launch_ms / 1e3) / 1e9
+    int_roofline = None
+    if field == "gl64":
+        rate = st.gl64_butterfly_rate(local)  # measured now, same arithmetic on registers
+        bfly = (n // 2) * lg  # butterflies per transform
+        got = bfly / (step_ms / 2 / 1e3)
+        int_roofline = {"bound": "int", "unit": "Gbutterfly/s", "achieved": got / 1e9, "peak": rate / 1e9,
+                        "frac": got / rate, "peak_kind": "measured (stntt_measure_gl64_butterfly_rate)",
+                        "butterflies_per_transform": bfly}
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                 "traffic": None, "peak_kind": hbm_kind,
                 "bytes_per_launch": bytes_per_launch, "launches_per_transform": passes,
@@ -547,7 +555,7 @@ def main():
             "config": {"workload": args.workload, "field": field, "n": n, "batch": 1,
                        "step": "forward + inverse, in place", "l2": "flushed between steps (256 MiB write)",
                        "parallelism": f"replicas x{world}"},
-            "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
+            "e2e": e2e, "roofline": roofline, "int_roofline": int_roofline, "cpu_baseline": cpu, "clocks": clocks,
             "gpu_launches": 2 * passes * args.steps, "round_trip_ok": ok,
         }
         print(json.dumps(line), flush=True)

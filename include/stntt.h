@@ -248,6 +248,13 @@ int stntt_server_destroy(stntt_server *sv);
 int stntt_ntt_gl64_noalloc(const uint64_t *d_in, uint64_t *d_out, uint32_t log_n, uint32_t batch, int dir,
                            stntt_stream stream);
 
+/* ---- integer roofline ---------------------------------------------------------- */
+/* Goldilocks butterflies per second (add, sub and one product per butterfly)
+ * that this GPU sustains on register-resident data, measured with the tile
+ * kernel's own arithmetic and CUDA events: the integer roofline for the
+ * transforms. Synchronous; about 10 ms. */
+int stntt_measure_gl64_butterfly_rate(int device, double *butterflies_per_s);
+
 /* ---- synthetic inputs ------------------------------------------------------------ */
 /* Uniform residues in [0,p) from a counter-based splitmix64 stream:
  * element i, attempt a: z = mix64(seed + 0x9E3779B97F4A7C15 * (i + (a << 40) + 1));

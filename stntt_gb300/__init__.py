@@ -119,6 +119,7 @@ _SIGS = {
     "stntt_batch_destroy": (_int, [_vp]),
     "stntt_selftest_wait_timeout": (_int, [_vp, _u32]),
     "stntt_clock_s": (C.c_double, []),
+    "stntt_measure_gl64_butterfly_rate": (_int, [_int, C.POINTER(C.c_double)]),
     "stntt_server_create": (_int, [_vp, C.POINTER(ServerConfig), C.POINTER(_vp)]),
     "stntt_server_submit": (_int, [_vp, C.POINTER(Request)]),
     "stntt_server_submit_at": (_int, [_vp, C.POINTER(Request), C.c_double]),
@@ -182,6 +183,13 @@ def params_u32(log_n: int) -> tuple[int, int]:
 def gl64_root(log_n: int) -> int:
     r = _u64()
     _check(lib().stntt_gl64_root(log_n, C.byref(r)))
+    return r.value
+
+
+def gl64_butterfly_rate(device: int = 0) -> float:
+    """Measured Goldilocks butterflies/s on register-resident data (integer roofline)."""
+    r = C.c_double()
+    _check(lib().stntt_measure_gl64_butterfly_rate(device, C.byref(r)))
     return r.value
 
 

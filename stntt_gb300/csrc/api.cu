@@ -26,9 +26,15 @@
 
 namespace stntt {
 
-cudaError_t launch_tile_u32(const PassDesc &, uint32_t, const void *, const void *, void *, uint64_t, cudaStream_t);
-cudaError_t launch_tile_gl64(const PassDesc &, uint32_t, const void *, const void *, void *, uint64_t,
-                             cudaStream_t);
+cudaError_t launch_tile_u32(const PassDesc &, uint32_t, const void *, const void *, void *, uint64_t, cudaStream_t,
+                             const void *);
+cudaError_t launch_tile_u32l(const PassDesc &, uint32_t, const void *, const void *, void *, uint64_t, cudaStream_t,
+                             const void *);
+cudaError_t batch_prepare_u32l(size_t, int *);
+cudaError_t batch_launch_u32l(const void *, const void *, unsigned long long, unsigned int *, void *, size_t, unsigned,
+                              unsigned, cudaStream_t);
+cudaError_t launch_tile_gl64(const PassDesc &, uint32_t, const void *, const void *, void *, uint64_t, cudaStream_t,
+                             const void *);
 cudaError_t gen_powers_u32(void *, uint64_t, uint64_t, uint64_t, uint32_t, cudaStream_t);
 cudaError_t gen_powers_gl64(void *, uint64_t, uint64_t, uint64_t, cudaStream_t);
 cudaError_t pointwise_u32(const void *, const void *, void *, size_t, uint32_t, cudaStream_t);
@@ -37,6 +43,7 @@ cudaError_t fill_uniform_u32(void *, size_t, uint64_t, uint32_t, cudaStream_t);
 cudaError_t fill_uniform_gl64(void *, size_t, uint64_t, cudaStream_t);
 cudaError_t copy_scale_u32(const void *, void *, size_t, uint64_t, uint32_t, cudaStream_t);
 cudaError_t copy_scale_gl64(const void *, void *, size_t, uint64_t, cudaStream_t);
+cudaError_t launch_gl_probe(uint64_t *, unsigned, int, cudaStream_t);
 size_t batch_args_size_u32();
 size_t batch_args_size_gl64();
 void batch_args_fill_u32(const PassDesc &, uint32_t, const void *, const unsigned long long *,
@@ -74,9 +81,12 @@ uint64_t host_tw_entry(int field, uint64_t w, uint32_t p) {
 }
 
 cudaError_t launch_tile(int field, const PassDesc &d, uint32_t p, const void *tables, const void *in, void *out,
-                        uint64_t batch, cudaStream_t s) {
-    return field == kFieldGL ? launch_tile_gl64(d, p, tables, in, out, batch, s)
-                             : launch_tile_u32(d, p, tables, in, out, batch, s);
+                        uint64_t batch, cudaStream_t s, const void *in2) {
+    if (field == kFieldGL)
+        return launch_tile_gl64(d, p, tables, in, out, batch, s, in2);
+    // lazy reduction needs 4p < 2^32
+    return p < (1u << 30) ? launch_tile_u32l(d, p, tables, in, out, batch, s, in2)
+                          : launch_tile_u32(d, p, tables, in, out, batch, s, in2);
 }
 cudaError_t launch_gen_powers(int field, void *out, uint64_t count, uint64_t base, uint64_t scale, uint32_t p,
                               cudaStream_t s) {
@@ -449,10 +459,15 @@ int check_u32_args(stntt_ctx *ctx, uint32_t log_n, uint32_t p, uint32_t root) {
 }
 
 // Run a plan: first pass reads `in`, last pass writes `out`.
-int run_plan(stntt_ctx *ctx, const Plan &pl, const void *in, void *out, uint64_t batch, cudaStream_t s) {
+int run_plan(stntt_ctx *ctx, const Plan &pl, const void *in, void *out, uint64_t batch, cudaStream_t s,
+             const void *in2) {
     const size_t esz = pl.field == kFieldGL ? 8 : 4;
     const size_t bytes = (batch << pl.log_n) * esz;
     if (pl.passes.empty()) {  // n == 1: the identity
+        if (in2) {
+            cudaError_t e = launch_pointwise(pl.field, in, in2, out, (size_t)batch << pl.log_n, pl.p, s);
+            return e == cudaSuccess ? STNTT_OK : cuda_fail(ctx, e, "pointwise launch");
+        }
         if (in != out) {
             cudaError_t e = cudaMemcpyAsync(out, in, bytes, cudaMemcpyDeviceToDevice, s);
             if (e != cudaSuccess)
@@ -468,9 +483,16 @@ int run_plan(stntt_ctx *ctx, const Plan &pl, const void *in, void *out, uint64_t
     }
     const size_t K = pl.passes.size();
     const void *src = in;
+    if (in2 && pl.passes[0].E > 16) {  // no fused kernel for this shape: separate pointwise product
+        cudaError_t e = launch_pointwise(pl.field, in, in2, out, (size_t)batch << pl.log_n, pl.p, s);
+        if (e != cudaSuccess)
+            return cuda_fail(ctx, e, "pointwise launch");
+        src = out;
+        in2 = nullptr;
+    }
     for (size_t i = 0; i < K; ++i) {
         void *dst = (i + 1 == K) ? out : ws;
-        cudaError_t e = launch_tile(pl.field, pl.passes[i], pl.p, pl.d_tables, src, dst, batch, s);
+        cudaError_t e = launch_tile(pl.field, pl.passes[i], pl.p, pl.d_tables, src, dst, batch, s, i == 0 ? in2 : nullptr);
         if (e != cudaSuccess)
             return cuda_fail(ctx, e, "tile kernel launch");
         src = dst;
@@ -1071,10 +1093,9 @@ int polymul_impl(stntt_ctx *ctx, int field, const void *a, const void *b, void *
         return rc;
     if ((rc = run_plan(ctx, *fwd, a, out, 1, s)))
         return rc;
-    cudaError_t e = launch_pointwise(field, out, tb, out, (size_t)1 << log_n, p, s);
-    if (e != cudaSuccess)
-        return cuda_fail(ctx, e, "pointwise launch");
-    return run_plan(ctx, *inv, out, out, 1, s);
+    // the pointwise product happens inside the inverse's first pass (it
+    // multiplies the two forward outputs as it loads them)
+    return run_plan(ctx, *inv, out, out, 1, s, tb);
 }
 }  // namespace sd
 extern "C" {
@@ -1115,6 +1136,52 @@ int stntt_fill_uniform_u32(uint32_t *d_out, size_t count, uint64_t seed, uint32_
                                                                                                       : STNTT_ECUDA;
 }
 
+int stntt_measure_gl64_butterfly_rate(int device, double *rate) {
+    if (!rate)
+        return STNTT_EINVAL;
+    DeviceGuard g(device);
+    if (g.err != cudaSuccess)
+        return STNTT_EINVAL;
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    const unsigned blocks = (unsigned)sms * 8, threads = 256;
+    const int reps = 100;
+    uint64_t *d = nullptr;
+    if (cudaMalloc(&d, (size_t)blocks * threads * 8) != cudaSuccess)
+        return STNTT_ENOMEM;
+    cudaStream_t s = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    if (e == cudaSuccess)
+        e = cudaEventCreate(&e0);
+    if (e == cudaSuccess)
+        e = cudaEventCreate(&e1);
+    float ms = 0;
+    if (e == cudaSuccess)
+        e = launch_gl_probe(d, blocks, 4, s);  // warm-up
+    if (e == cudaSuccess)
+        e = cudaEventRecord(e0, s);
+    if (e == cudaSuccess)
+        e = launch_gl_probe(d, blocks, reps, s);
+    if (e == cudaSuccess)
+        e = cudaEventRecord(e1, s);
+    if (e == cudaSuccess)
+        e = cudaEventSynchronize(e1);
+    if (e == cudaSuccess)
+        e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e0)
+        cudaEventDestroy(e0);
+    if (e1)
+        cudaEventDestroy(e1);
+    if (s)
+        cudaStreamDestroy(s);
+    cudaFree(d);
+    if (e != cudaSuccess || ms <= 0)
+        return STNTT_ECUDA;
+    *rate = (double)blocks * threads * reps * 32.0 / (ms * 1e-3);  // 32 butterflies per repetition
+    return STNTT_OK;
+}
+
 int stntt_fill_uniform_gl64(uint64_t *d_out, size_t count, uint64_t seed, stntt_stream stream) {
     if (!d_out && count)
         return STNTT_EINVAL;
@@ -1145,6 +1212,7 @@ constexpr unsigned kDefaultSpinLimit = 5000000;  // polls of ~200 ns: about one 
 
 struct BatchPart {
     int field = 0;
+    bool lazy = false;  // 32-bit field: every job's p < 2^30
     void *d_buf = nullptr;
     size_t args_off = 0, items_off = 0, counters_off = 0, ctl_off = 0, ptr_off = 0, bytes = 0;
     unsigned long long nitems = 0;
@@ -1272,6 +1340,10 @@ int build_part(stntt_ctx *ctx, stntt_batch *bt, int field, const std::vector<con
     }
     BatchPart part;
     part.field = field;
+    part.lazy = field == kFieldU32;
+    for (const stntt_job *j : jobs)
+        if (field == kFieldU32 && j->p >= (1u << 30))
+            part.lazy = false;
     part.nitems = phaseA.size() + phaseB.size();
     part.ncounters = std::max<uint32_t>(njob2, 1);
     part.smem = smem;
@@ -1302,7 +1374,8 @@ int build_part(stntt_ctx *ctx, stntt_batch *bt, int field, const std::vector<con
     if (e != cudaSuccess)
         return cuda_fail(ctx, e, "batch work list upload");
     int bps = 0;
-    e = field == kFieldGL ? batch_prepare_gl64(P.smem, &bps) : batch_prepare_u32(P.smem, &bps);
+    e = field == kFieldGL ? batch_prepare_gl64(P.smem, &bps)
+                          : (P.lazy ? batch_prepare_u32l(P.smem, &bps) : batch_prepare_u32(P.smem, &bps));
     if (e != cudaSuccess || bps < 1)
         return fail(ctx, STNTT_ECUDA, "batch kernel does not fit on an SM");
     int dev = 0, sms = 0;
@@ -1402,9 +1475,10 @@ int stntt_batch_launch(stntt_batch *b, stntt_stream stream) {
                     ? batch_launch_gl64(base + P.args_off, base + P.items_off, P.nitems,
                                         reinterpret_cast<unsigned int *>(base + P.counters_off), base + P.ctl_off,
                                         P.smem, P.grid, b->spin_limit, s)
-                    : batch_launch_u32(base + P.args_off, base + P.items_off, P.nitems,
-                                       reinterpret_cast<unsigned int *>(base + P.counters_off), base + P.ctl_off,
-                                       P.smem, P.grid, b->spin_limit, s);
+                    : (P.lazy ? batch_launch_u32l : batch_launch_u32)(
+                          base + P.args_off, base + P.items_off, P.nitems,
+                          reinterpret_cast<unsigned int *>(base + P.counters_off), base + P.ctl_off, P.smem, P.grid,
+                          b->spin_limit, s);
         if (e != cudaSuccess)
             return cuda_fail(ctx, e, "batch launch");
     }

@@ -15,7 +15,9 @@ struct Plan;
 // Twiddle tables and pass list for one transform (built and cached on first use).
 int get_plan(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t p, uint64_t root, int dir, const Plan **out);
 // Run a plan: first pass reads `in`, last pass writes `out`, on stream s.
-int run_plan(stntt_ctx *ctx, const Plan &pl, const void *in, void *out, uint64_t batch, cudaStream_t s);
+// in2: optional second input whose product with `in` the first pass transforms.
+int run_plan(stntt_ctx *ctx, const Plan &pl, const void *in, void *out, uint64_t batch, cudaStream_t s,
+             const void *in2 = nullptr);
 // Per-stream scratch of at least `bytes` (grows with a synchronising cudaMalloc).
 int get_workspace(stntt_ctx *ctx, cudaStream_t s, size_t bytes, void **ptr);
 // Free the workspace of a stream that is about to be destroyed.

@@ -37,6 +37,36 @@ struct FieldU32 {
     // General product of two residues (pointwise products).
     __device__ __forceinline__ T mul(T a, T b) const { return (uint32_t)(((uint64_t)a * b) % p); }
     __device__ __forceinline__ static T tw_value(TW w) { return w.x; }
+    // difference that only feeds a twiddle product; canonical form for storing
+    __device__ __forceinline__ T sub_lazy(T a, T b) const { return sub(a, b); }
+    __device__ __forceinline__ T canon(T a) const { return a; }
+};
+
+// The same field for p < 2^30 with lazy reduction (Harvey's butterflies):
+// values rest in [0, 2p); a difference that feeds a product is a - b + 2p in
+// [0, 4p) (one add); Shoup products of any input below 2^32 land in [0, 2p)
+// without a correction; canon() maps [0, 2p) to [0, p) before HBM stores.
+struct FieldU32L {
+    using T = uint32_t;
+    using TW = uint2;
+    uint32_t p;
+
+    __device__ __forceinline__ T add(T a, T b) const {
+        const uint32_t s = a + b;
+        return min(s, s - 2 * p);
+    }
+    __device__ __forceinline__ T sub(T a, T b) const {
+        const uint32_t d = a - b + 2 * p;
+        return min(d, d - 2 * p);
+    }
+    __device__ __forceinline__ T sub_lazy(T a, T b) const { return a - b + 2 * p; }
+    __device__ __forceinline__ T mul_tw(T a, TW w) const {
+        const uint32_t q = __umulhi(a, w.y);
+        return a * w.x - q * p;
+    }
+    __device__ __forceinline__ T mul(T a, T b) const { return (uint32_t)(((uint64_t)a * b) % p); }
+    __device__ __forceinline__ static T tw_value(TW w) { return w.x; }
+    __device__ __forceinline__ T canon(T a) const { return min(a, a - p); }
 };
 
 struct FieldGL {
@@ -127,6 +157,8 @@ struct FieldGL {
     }
     __device__ __forceinline__ T mul_tw(T a, TW w) const { return mul(a, w); }
     __device__ __forceinline__ static T tw_value(TW w) { return w; }
+    __device__ __forceinline__ T sub_lazy(T a, T b) const { return sub(a, b); }
+    __device__ __forceinline__ T canon(T a) const { return a; }
 };
 
 }  // namespace stntt

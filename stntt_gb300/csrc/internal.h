@@ -25,7 +25,7 @@ struct PassDesc {
 
 // ---- launchers (return the CUDA error of the launch) ----------------------
 cudaError_t launch_tile(int field, const PassDesc &d, uint32_t p, const void *tables, const void *in, void *out,
-                        uint64_t batch, cudaStream_t s);
+                        uint64_t batch, cudaStream_t s, const void *in2 = nullptr);
 // out[i] = scale * base^i, i < count, as twiddle entries (u32: Shoup pairs).
 cudaError_t launch_gen_powers(int field, void *out, uint64_t count, uint64_t base, uint64_t scale, uint32_t p,
                               cudaStream_t s);

@@ -16,9 +16,9 @@ __device__ __forceinline__ typename F::TW to_tw(uint64_t raw) {
     return w;
 }
 
-template <class F, int E, int TAIL>
+template <class F, int E, int TAIL, bool IN2 = false>
 cudaError_t launch_tile_e(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks, cudaStream_t s) {
-    auto kern = tile_kernel<F, E, TAIL>;
+    auto kern = tile_kernel<F, E, TAIL, IN2>;
     static bool attr_set[64] = {};  // per device: the opt-in shared-memory size of this kernel
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -66,14 +66,16 @@ void fill_args(TileArgs<F> &a, const PassDesc &d, uint32_t p, const void *tables
     a.cs = d.cs;
     a.in_ptrs = nullptr;
     a.out_ptrs = nullptr;
+    a.in2 = nullptr;
     a.total = 0;
 }
 
 template <class F>
 cudaError_t launch_tile_t(const PassDesc &d, uint32_t p, const void *tables, const void *in, void *out,
-                          uint64_t batch, cudaStream_t s) {
+                          uint64_t batch, cudaStream_t s, const void *in2 = nullptr) {
     TileArgs<F> a;
     fill_args<F>(a, d, p, tables, in, out);
+    a.in2 = static_cast<const typename F::T *>(in2);
     const uint64_t rows = batch << (d.logN - d.logL);
     a.total = rows;
     const uint64_t blocks = (rows + (1ull << d.logC) - 1) >> d.logC;
@@ -82,6 +84,21 @@ cudaError_t launch_tile_t(const PassDesc &d, uint32_t p, const void *tables, con
     if (blocks > 0x7fffffffull)
         return cudaErrorInvalidConfiguration;
     const uint32_t tail = d.logL & 3;
+    if (in2) {  // fused pointwise product: instantiated for up to 16 elements per thread
+        switch (d.E) {
+        case 2: return launch_tile_e<F, 2, 1, true>(d, a, blocks, s);
+        case 4: return launch_tile_e<F, 4, 2, true>(d, a, blocks, s);
+        case 8: return launch_tile_e<F, 8, 3, true>(d, a, blocks, s);
+        case 16:
+            switch (tail) {
+            case 0: return launch_tile_e<F, 16, 0, true>(d, a, blocks, s);
+            case 1: return launch_tile_e<F, 16, 1, true>(d, a, blocks, s);
+            case 2: return launch_tile_e<F, 16, 2, true>(d, a, blocks, s);
+            default: return launch_tile_e<F, 16, 3, true>(d, a, blocks, s);
+            }
+        default: return cudaErrorNotSupported;
+        }
+    }
     switch (d.E) {
     case 2: return launch_tile_e<F, 2, 1>(d, a, blocks, s);
     case 4: return launch_tile_e<F, 4, 2>(d, a, blocks, s);

@@ -33,8 +33,8 @@ __global__ void fill_uniform_gl64_kernel(uint64_t *out, size_t count, uint64_t s
 }
 
 cudaError_t launch_tile_gl64(const PassDesc &d, uint32_t p, const void *tables, const void *in, void *out,
-                             uint64_t batch, cudaStream_t s) {
-    return launch_tile_t<FieldGL>(d, p, tables, in, out, batch, s);
+                    uint64_t batch, cudaStream_t s, const void *in2) {
+    return launch_tile_t<FieldGL>(d, p, tables, in, out, batch, s, in2);
 }
 
 cudaError_t gen_powers_gl64(void *out, uint64_t count, uint64_t base, uint64_t scale, cudaStream_t s) {
@@ -73,6 +73,56 @@ cudaError_t batch_prepare_gl64(size_t smem, int *blocks_per_sm) { return batch_p
 cudaError_t batch_launch_gl64(const void *args, const void *items, unsigned long long nitems, unsigned int *counters,
                              void *ctl, size_t smem, unsigned grid, unsigned spin_limit, cudaStream_t s) {
     return batch_launch_t<FieldGL>(args, items, nitems, counters, ctl, smem, grid, spin_limit, s);
+}
+
+}  // namespace stntt
+
+// ---- integer throughput probe ------------------------------------------------
+// The tile kernel's arithmetic without its memory traffic: every thread runs
+// the radix-16 step (15 twiddle products, then the 16-point DIF network with
+// 17 products) on 16 register values, `reps` times, and writes one checksum.
+// Measures the Goldilocks butterfly rate this GPU sustains: the integer
+// roofline the NTT kernels are compared with.
+namespace stntt {
+
+__global__ void __launch_bounds__(256) gl_butterfly_probe(uint64_t *out, int reps, uint64_t w1, uint64_t w2,
+                                                          uint64_t w3) {
+    FieldGL f;
+    uint64_t x[16];
+    uint64_t seed = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * 0x9E3779B97F4A7C15ull + 1;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        seed = seed * 6364136223846793005ull + 1442695040888963407ull;
+        x[i] = seed >> 1;  // < 2^63 < p
+    }
+    const uint64_t w[8] = {1, w1, w2, w3, w1 ^ 5, w2 ^ 7, w3 ^ 9, w1 ^ 11};
+    for (int r = 0; r < reps; ++r) {
+#pragma unroll
+        for (int i = 1; i < 16; ++i)
+            x[i] = f.mul(x[i], w[i & 7]);
+#pragma unroll
+        for (int h = 8; h >= 1; h >>= 1)
+#pragma unroll
+            for (int base = 0; base < 16; base += 2 * h)
+#pragma unroll
+                for (int j = 0; j < h; ++j) {
+                    const uint64_t a = x[base + j], b = x[base + j + h];
+                    x[base + j] = f.add(a, b);
+                    const uint64_t d = f.sub(a, b);
+                    x[base + j + h] = j == 0 ? d : f.mul(d, w[j * (16 / (2 * h))]);
+                }
+    }
+    uint64_t acc = 0;
+#pragma unroll
+    for (int i = 0; i < 16; ++i)
+        acc ^= x[i] * (uint64_t)(i + 1);
+    out[(uint64_t)blockIdx.x * blockDim.x + threadIdx.x] = acc;
+}
+
+cudaError_t launch_gl_probe(uint64_t *out, unsigned blocks, int reps, cudaStream_t s) {
+    gl_butterfly_probe<<<blocks, 256, 0, s>>>(out, reps, 0x1234567890ABCDEFull % FieldGL::P,
+                                               0xFEDCBA9876543210ull % FieldGL::P, 0x0F0F0F0F0F0F0F0Full);
+    return cudaGetLastError();
 }
 
 }  // namespace stntt

@@ -51,12 +51,19 @@ struct TileArgs {
     // from in_ptrs[b] and writes to out_ptrs[b] instead of in/out + b*n.
     const unsigned long long *in_ptrs;
     const unsigned long long *out_ptrs;
+    // Optional second input (pointwise product fused into the first step):
+    // the pass transforms in[j] * in2[j] (same layout as in).
+    const T *in2;
 };
 
 template <class F>
 struct Pad;
 template <>
 struct Pad<FieldU32> {
+    static __device__ __forceinline__ uint32_t at(uint32_t i) { return i + (i >> 5); }
+};
+template <>
+struct Pad<FieldU32L> {
     static __device__ __forceinline__ uint32_t at(uint32_t i) { return i + (i >> 5); }
 };
 template <>
@@ -84,8 +91,10 @@ __device__ __forceinline__ void dft_reg(const F &f, typename F::T *x, const type
             for (int j = 0; j < h; ++j) {
                 const typename F::T a = x[base + j], b = x[base + j + h];
                 x[base + j] = f.add(a, b);
-                const typename F::T d = f.sub(a, b);
-                x[base + j + h] = (j == 0) ? d : f.mul_tw(d, w16[j * (16 / (2 * h))]);
+                if (j == 0)
+                    x[base + j + h] = f.sub(a, b);
+                else
+                    x[base + j + h] = f.mul_tw(f.sub_lazy(a, b), w16[j * (16 / (2 * h))]);
             }
         }
     }
@@ -93,13 +102,14 @@ __device__ __forceinline__ void dft_reg(const F &f, typename F::T *x, const type
 
 template <class T>
 struct Geo {
-    const T *src;  // element j of this column/row: src[j * istride]
+    const T *src;   // element j of this column/row: src[j * istride]
+    const T *src2;  // second input for the fused pointwise product, or null
     T *dst;        // element k: dst[k * ostride]
     uint64_t istride, ostride, col;
     bool valid;  // false for the padding rows of a partial last CTA
 };
 
-template <class F, int E, int LOGR, bool first, bool last>
+template <class F, int E, int LOGR, bool first, bool last, bool in2 = false>
 __device__ __forceinline__ void tile_step(const TileArgs<F> &a, const F &f, typename F::T (&x)[E],
                                           typename F::T *sm, uint32_t c, uint32_t u, uint32_t logp,
                                           const Geo<typename F::T> &g) {
@@ -116,8 +126,13 @@ __device__ __forceinline__ void tile_step(const TileArgs<F> &a, const F &f, type
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             const uint32_t idx = t + r * T_;
-            if constexpr (first)
+            if constexpr (first) {
                 x[m * R + r] = g.valid ? g.src[(uint64_t)idx * g.istride] : T(0);
+                if constexpr (in2) {
+                    if (g.valid)
+                        x[m * R + r] = f.mul(x[m * R + r], g.src2[(uint64_t)idx * g.istride]);
+                }
+            }
             else
                 x[m * R + r] = col_sm[Pad<F>::at(idx)];
         }
@@ -156,6 +171,7 @@ __device__ __forceinline__ void tile_step(const TileArgs<F> &a, const F &f, type
                 } else if (a.do_scale) {
                     v = f.mul_tw(v, a.scale);
                 }
+                v = f.canon(v);
                 if (g.valid)
                     g.dst[(uint64_t)pos * g.ostride] = v;
             } else {
@@ -167,10 +183,35 @@ __device__ __forceinline__ void tile_step(const TileArgs<F> &a, const F &f, type
         __syncthreads();
 }
 
+// The first step of a tile (the optional radix-2/4/8 step, else radix 16).
+// Returns true when it was also the last step.
+template <class F, int E, int TAIL, bool IN2>
+__device__ __forceinline__ bool first_step(const TileArgs<F> &a, const F &f, typename F::T (&x)[E],
+                                           typename F::T *sm, uint32_t c, uint32_t u, const Geo<typename F::T> &g,
+                                           uint32_t &logp) {
+    const int n16 = (int)(a.logL >> 2);
+    if constexpr (TAIL > 0) {
+        if (n16 == 0) {
+            tile_step<F, E, TAIL, true, true, IN2>(a, f, x, sm, c, u, 0, g);
+            return true;
+        }
+        tile_step<F, E, TAIL, true, false, IN2>(a, f, x, sm, c, u, 0, g);
+        logp = TAIL;
+    } else {
+        if (n16 == 1) {
+            tile_step<F, E, 4, true, true, IN2>(a, f, x, sm, c, u, 0, g);
+            return true;
+        }
+        tile_step<F, E, 4, true, false, IN2>(a, f, x, sm, c, u, 0, g);
+        logp = 4;
+    }
+    return false;
+}
+
 // One CTA's worth of work: C columns (COL) or rows (ROW) with global index
 // blk * C + c over the batch. Used by tile_kernel (blk = blockIdx.x) and by
 // the persistent batched kernel (blk from its work list).
-template <class F, int E, int TAIL>
+template <class F, int E, int TAIL, bool IN2 = false>
 __device__ __forceinline__ void tile_run(const TileArgs<F> &a, uint64_t blk, typename F::T *sm) {
     using T = typename F::T;
     F f;
@@ -200,16 +241,22 @@ __device__ __forceinline__ void tile_run(const TileArgs<F> &a, uint64_t blk, typ
         ibase = reinterpret_cast<const T *>(a.in_ptrs[b]);
         obase = reinterpret_cast<T *>(a.out_ptrs[b]);
     }
+    const T *ibase2 = a.in2 ? a.in2 + (b << a.logN) : nullptr;
+    g.src2 = nullptr;
     if (a.mode == kModeCol) {
         const uint64_t q = rem >> a.logS;
         g.col = rem & ((1ull << a.logS) - 1);
         g.src = ibase + (q << a.logM) + g.col;
+        if (ibase2)
+            g.src2 = ibase2 + (q << a.logM) + g.col;
         g.dst = obase + (q << a.logM) + g.col;
         g.istride = g.ostride = 1ull << a.logS;
     } else {
         const uint64_t inrow = ((rem & ((1ull << a.logN1) - 1)) << a.logN2) + (rem >> a.logN1);
         g.col = 0;
         g.src = ibase + (inrow << a.logL);
+        if (ibase2)
+            g.src2 = ibase2 + (inrow << a.logL);
         g.istride = 1;
         g.dst = obase + rem;
         g.ostride = 1ull << logPer;
@@ -218,21 +265,9 @@ __device__ __forceinline__ void tile_run(const TileArgs<F> &a, uint64_t blk, typ
     T x[E];
     const int n16 = (int)(a.logL >> 2);  // radix-16 steps after the optional leading step
     uint32_t logp = 0;
-    if constexpr (TAIL > 0) {
-        if (n16 == 0) {
-            tile_step<F, E, TAIL, true, true>(a, f, x, sm, c, u, 0, g);
-            return;
-        }
-        tile_step<F, E, TAIL, true, false>(a, f, x, sm, c, u, 0, g);
-        logp = TAIL;
-    } else {
-        if (n16 == 1) {
-            tile_step<F, E, 4, true, true>(a, f, x, sm, c, u, 0, g);
-            return;
-        }
-        tile_step<F, E, 4, true, false>(a, f, x, sm, c, u, 0, g);
-        logp = 4;
-    }
+    // the first step (with the fused pointwise product when IN2)
+    if (first_step<F, E, TAIL, IN2>(a, f, x, sm, c, u, g, logp))
+        return;
     if constexpr (E >= 16) {
         const int mid = n16 - (TAIL > 0 ? 1 : 2);  // radix-16 steps between the first and the last
         for (int s = 0; s < mid; ++s) {
@@ -243,10 +278,10 @@ __device__ __forceinline__ void tile_run(const TileArgs<F> &a, uint64_t blk, typ
     }
 }
 
-template <class F, int E, int TAIL>
+template <class F, int E, int TAIL, bool IN2 = false>
 __global__ void __launch_bounds__(E >= 32 ? 512 : 1024) tile_kernel(const TileArgs<F> a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    tile_run<F, E, TAIL>(a, blockIdx.x, reinterpret_cast<typename F::T *>(smem_raw));
+    tile_run<F, E, TAIL, IN2>(a, blockIdx.x, reinterpret_cast<typename F::T *>(smem_raw));
 }
 
 }  // namespace stntt

@@ -337,3 +337,26 @@ def test_argument_errors(ctx):
     p, root = st.params_u32(4)
     ctx.ntt_u32(d, 4, 1, p, root)
     assert not host32(d).any()
+
+
+@pytest.mark.parametrize("lg", [3, 10, 14, 20])
+def test_u32_primes_above_2e30(ctx, lg):
+    """Primes in [2^30, 2^31) take the strict-reduction kernels (the lazy ones
+    need 4p < 2^32)."""
+    root, p = st.findParams(1 << lg, 1 << 30)
+    assert (1 << 30) <= p < (1 << 31)
+    x = O.uniform_u32(9 + lg, p, 2 << lg)
+    d = dev32(x)
+    ctx.ntt_u32(d, lg, 2, p, root)
+    assert np.array_equal(host32(d), O.ntt_u32(x, root, p, batch=2))
+    ctx.ntt_u32(d, lg, 2, p, root, inverse=True)
+    assert np.array_equal(host32(d), x)
+    a = np.zeros(1 << lg, np.uint32)
+    b = np.zeros(1 << lg, np.uint32)
+    h = max(1, (1 << lg) // 2)
+    a[:h], b[:h] = O.uniform_u32(1, p, h), O.uniform_u32(2, p, h)
+    out = torch.empty(1 << lg, dtype=torch.int32, device="cuda")
+    ctx.polymul_u32(dev32(a), dev32(b), out, lg, p, root)
+    if lg <= 10:
+        want = O.polymul_u32(a[:h], b[:h], p)
+        assert np.array_equal(host32(out)[: want.size], want)
