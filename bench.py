@@ -61,6 +61,7 @@ def parse():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--mix-jobs", type=int, default=4096, help="jobs in the batched mix (4096 for the headline)")
     return ap.parse_args()
 
 
@@ -69,6 +70,18 @@ def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return rank, world, local
+
+
+def max_over_ranks(value: float, world: int, device=None) -> float:
+    """The largest `value` over all ranks (timings: the slowest rank counts)."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
 def peaks():
@@ -218,11 +231,11 @@ def cpu_baseline(field: str, lg: int):
 MIX_JOBS, MIX_LO, MIX_HI, MIX_SEED = 4096, 10, 18, 0x57170001 + 3
 
 
-def mix_sizes():
+def mix_sizes(jobs: int = MIX_JOBS):
     """log2 n of each job: uniform in [10, 18] from a fixed seed; job i is
     forward for even i and inverse for odd i."""
     rng = np.random.default_rng(MIX_SEED)
-    return [int(v) for v in rng.integers(MIX_LO, MIX_HI + 1, MIX_JOBS)]
+    return [int(v) for v in rng.integers(MIX_LO, MIX_HI + 1, jobs)]
 
 
 def run_batch_mix(args):
@@ -237,7 +250,7 @@ def run_batch_mix(args):
         dist.init_process_group("nccl", device_id=dev)
     import stntt_gb300 as st
 
-    sizes = mix_sizes()
+    sizes = mix_sizes(args.mix_jobs)
     total = sum(1 << s for s in sizes)
     data = torch.empty(total, dtype=torch.int64, device=dev)
     st.fill_uniform_gl64(data, 77 + rank)
@@ -274,9 +287,7 @@ def run_batch_mix(args):
     ok = ok and b.status() == 0
     ms = e0.elapsed_time(e1) / args.steps
     if world > 1:
-        t = torch.tensor([ms], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = max_over_ranks(ms, world, dev)
     value = world * total / (ms / 1e3) / 1e9
     # one launch sequence per transform (the comparison), plain launches
     s2 = torch.cuda.current_stream()
@@ -298,7 +309,7 @@ def run_batch_mix(args):
             "value": value, "unit": "Gelem/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
             "data": "synthetic (splitmix64 uniform residues)",
-            "config": {"workload": "gl64_batch_mix", "jobs": MIX_JOBS, "log_n_range": [MIX_LO, MIX_HI],
+            "config": {"workload": "gl64_batch_mix", "jobs": len(sizes), "log_n_range": [MIX_LO, MIX_HI],
                        "seed": MIX_SEED, "elements": total, "directions": "alternating forward / inverse",
                        "launch": "one persistent launch replayed from a CUDA graph", **info},
             "per_call": {"value": world * total / (per_ms / 1e3) / 1e9, "ms_per_step": per_ms,
@@ -478,9 +489,7 @@ def main():
     step_ms = float(np.sum(t_fwd) + np.sum(t_inv)) / args.steps
     total_ms = step_ms * args.steps
     if world > 1:
-        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+        total_ms = max_over_ranks(total_ms, world, dev)
         step_ms = total_ms / args.steps
     value = world * 2 * n * args.steps / (total_ms / 1e3) / 1e9
 

@@ -76,6 +76,7 @@ def lib():
         _bind(L, "orc_dft_gl64", None, [_u64p, _u64p, u32, u64])
         _bind(L, "orc_polymul_u32", None, [_u32p, sz, _u32p, sz, u32, _u32p])
         _bind(L, "orc_polymul_gl64", None, [_u64p, sz, _u64p, sz, _u64p])
+        _bind(L, "orc_fnv1a64", u64, [C.c_void_p, sz])
         _lib = L
     return _lib
 
@@ -219,6 +220,11 @@ def intt_gs_u32(vec, root: int, mod: int) -> np.ndarray:
     if lib().orc_intt_gs_u32(v, v.size, root, mod):
         raise RuntimeError("orc_intt_gs_u32 failed")
     return v
+
+
+def fnv1a64(a: np.ndarray) -> int:
+    b = np.ascontiguousarray(a)
+    return lib().orc_fnv1a64(b.ctypes.data, b.nbytes)
 
 
 def cpu_count() -> int:
