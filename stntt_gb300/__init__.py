@@ -20,6 +20,7 @@ CUDA library is missing or fails.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import platform
 from pathlib import Path
 from typing import Iterable, Optional, Sequence
@@ -233,11 +234,15 @@ def _stream(stream) -> int:
 class Context:
     """A ``stntt_ctx``: twiddle tables, plans and workspaces on one device."""
 
-    def __init__(self, device: int = 0):
+    def __init__(self, device: int = 0, tuned: bool = True):
         h = _vp()
         _check(lib().stntt_init(C.byref(h), device))
         self._h = h.value
         self.device = device
+        if tuned and os.environ.get("STNTT_NO_TUNED_PLANS") != "1":
+            from . import tune
+
+            tune.apply_cache(self)  # the autotuner's plans for this GPU, if any
 
     @classmethod
     def default(cls, device: int = 0) -> "Context":

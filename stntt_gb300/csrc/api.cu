@@ -251,7 +251,8 @@ uint64_t fmul(int field, uint64_t a, uint64_t b, uint32_t p) {
 void shape_pass(PassDesc &d, int field, uint64_t col_limit, uint32_t want_E, uint32_t want_C) {
     const uint32_t L = 1u << d.logL;
     // Defaults from the autotuner's sweeps on GB300 (both fields, 2^16..2^26):
-    // 16 elements per thread, C = min(8, 8192 / L) columns per CTA.
+    // 16 elements per thread, C = min(8, 8192 / L) columns per CTA for 8-byte
+    // values and min(16, 8192 / L) for 4-byte ones (64-byte row segments).
     d.E = L < 16 ? L : 16;
     if (L >= 16 && (want_E == 16 || want_E == 32) && want_E <= L)
         d.E = want_E;
@@ -263,7 +264,7 @@ void shape_pass(PassDesc &d, int field, uint64_t col_limit, uint32_t want_E, uin
     } else if (d.mode == kModeRow && d.logN == d.logL) {
         C = std::max<uint64_t>(1, 256 / U);  // whole transforms per CTA: ~256 threads
     } else {
-        C = std::min<uint64_t>(8, 8192 / L);
+        C = std::min<uint64_t>(field == kFieldGL ? 8 : 16, 8192 / L);
     }
     C = std::min<uint64_t>(C, max_threads / U);
     C = std::min<uint64_t>(C, col_limit);

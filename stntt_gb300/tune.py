@@ -24,6 +24,9 @@ from typing import Iterable
 import stntt_gb300 as st
 
 DEFAULT_CACHE = Path(os.environ.get("STNTT_TUNE_CACHE", str(Path.home() / ".cache" / "stntt_gb300" / "plans.json")))
+# Plans the tuner chose on this project's GB300s, keyed "name|SM count" (no driver):
+# applied to every new Context on a matching device unless STNTT_NO_TUNED_PLANS=1.
+PACKAGED = Path(__file__).resolve().parent / "tuned_plans.json"
 
 
 def splits(log_n: int, max_pass: int = 13) -> list[list[int]]:
@@ -130,9 +133,16 @@ def save_cache(cache: dict, path: Path = DEFAULT_CACHE) -> None:
     os.replace(tmp, path)
 
 
+def _device_class(key: str) -> str:
+    return "|".join(key.split("|")[:2])  # GPU name | SM count
+
+
 def apply_cache(ctx: st.Context, path: Path = DEFAULT_CACHE) -> int:
-    """Set every cached plan for this device on `ctx`; returns how many."""
-    entries = load_cache(path).get(_key(ctx.device), {})
+    """Set every cached plan for this device on `ctx`; returns how many.
+    Exact device keys win; otherwise the packaged plans for the device class."""
+    key = _key(ctx.device)
+    entries = dict(load_cache(PACKAGED).get(_device_class(key), {}))
+    entries.update(load_cache(path).get(key, {}))
     k = 0
     for name, e in entries.items():
         field_s, lg = name.split(":")
@@ -151,6 +161,17 @@ def record(ctx: st.Context, field: int, log_n: int, best: dict, path: Path = DEF
     save_cache(cache, path)
 
 
+def package(cache: Path, out: Path = PACKAGED) -> None:
+    """Fold a tuner cache into the packaged plans (keyed by device class)."""
+    src = load_cache(cache)
+    dst = load_cache(out)
+    for key, entries in src.items():
+        cls = dst.setdefault(_device_class(key), {})
+        for name, e in entries.items():
+            cls[name] = {k: e[k] for k in ("logs", "E", "C", "us")}
+    save_cache(dst, out)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--field", choices=["gl64", "u32"], default="gl64")
@@ -160,6 +181,7 @@ def main() -> None:
     ap.add_argument("--cache", default=str(DEFAULT_CACHE))
     ap.add_argument("--verbose", action="store_true")
     ap.add_argument("--out", default=None, help="also write all timings here (JSON)")
+    ap.add_argument("--package", action="store_true", help="fold the results into the packaged plans")
     args = ap.parse_args()
     field = st.FIELD_GL64 if args.field == "gl64" else st.FIELD_U32
     ctx = st.Context(0)
@@ -171,6 +193,8 @@ def main() -> None:
         print(json.dumps({"size": f"{args.field}:{lg}", "best": best, "candidates": len(res)}), flush=True)
     if args.out:
         Path(args.out).write_text(json.dumps(allres, indent=1))
+    if args.package:
+        package(Path(args.cache))
     ctx.close()
 
 
