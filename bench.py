@@ -62,6 +62,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--mix-jobs", type=int, default=4096, help="jobs in the batched mix (4096 for the headline)")
+    ap.add_argument("--streams", type=int, default=32, help="serving: request slots")
     return ap.parse_args()
 
 
@@ -70,6 +71,14 @@ def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return rank, world, local
+
+
+def ncu_traffic(workload: str):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
+    try:
+        return json.loads((ROOT / "profiles" / "ncu_traffic.json").read_text())[workload]["bytes_per_launch"]
+    except (OSError, KeyError, ValueError):
+        return None
 
 
 def max_over_ranks(value: float, world: int, device=None) -> float:
@@ -363,7 +372,7 @@ def run_serve_mix(args):
                 a2.numpy()[n // 2:] = 0
             pool[(gl, lg)] = (a, a2, b, o)
     ctx = st.Context(local)
-    sv = st.Server(ctx, streams=16, max_log_n=SERVE_HI, prewarm=(SERVE_LO, SERVE_HI))
+    sv = st.Server(ctx, streams=args.streams, max_log_n=SERVE_HI, prewarm=(SERVE_LO, SERVE_HI))
     reqs = []
     for i in range(count):
         lg, gl = int(logs[i]), bool(gls[i])
@@ -400,7 +409,7 @@ def run_serve_mix(args):
             "vs_baseline": None, "dtype": "u32+u64", "data": "synthetic (splitmix64 residues, seeded Poisson trace)",
             "config": {"workload": "serve_mix", "requests": count, "rate_per_s": SERVE_RATE,
                        "log_n_range": [SERVE_LO, SERVE_HI], "polymul_fraction": 0.3, "fields": "50/50",
-                       "streams": 16, "seed": SERVE_SEED},
+                       "streams": args.streams, "seed": SERVE_SEED},
             "latency_ms": {"p50": float(np.percentile(lat, 50)), "p90": float(np.percentile(lat, 90)),
                            "p99": float(np.percentile(lat, 99)), "max": float(lat.max()),
                            "queue_p50": float(np.percentile(qwait, 50)),
@@ -507,7 +516,8 @@ def main():
                         "frac": got / rate, "peak_kind": "measured (stntt_measure_gl64_butterfly_rate)",
                         "butterflies_per_transform": bfly}
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                "traffic": None, "peak_kind": hbm_kind,
+                "traffic": ncu_traffic(args.workload), "traffic_source": "ncu dram read+write per launch, profiles/",
+                "peak_kind": hbm_kind,
                 "bytes_per_launch": bytes_per_launch, "launches_per_transform": passes,
                 "pass_log_lengths": pass_logs, "mean_launch_us": launch_ms * 1e3,
                 "b_alg_per_transform": passes * bytes_per_launch if passes > 1 else 2 * n * esz,

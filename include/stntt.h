@@ -210,7 +210,7 @@ typedef struct stntt_completion {
     double submit_s, start_s, done_s; /* stntt_clock_s() at submit, admission, completion */
 } stntt_completion;
 typedef struct stntt_server_config {
-    uint32_t streams;      /* request slots (CUDA streams); 0 = 16 */
+    uint32_t streams;      /* request slots (CUDA streams); 0 = 32 */
     uint32_t max_log_n;    /* largest request; per-slot workspaces are sized for it; 0 = 22 */
     uint64_t arena_bytes;  /* device memory for operands; 0 = a quarter of free HBM, at most 8 GiB */
     uint32_t prewarm_min_log_n, prewarm_max_log_n; /* build twiddle tables for this range at start */

@@ -392,7 +392,7 @@ class Batch:
 class Server:
     """A ``stntt_server``: the request loop (see include/stntt.h)."""
 
-    def __init__(self, ctx: Context, streams: int = 16, max_log_n: int = 22, arena_bytes: int = 0,
+    def __init__(self, ctx: Context, streams: int = 32, max_log_n: int = 22, arena_bytes: int = 0,
                  prewarm: tuple[int, int] | None = None):
         cfg = ServerConfig(streams, max_log_n, arena_bytes, *(prewarm or (0, 0)))
         h = _vp()

@@ -35,8 +35,8 @@ struct BatchCtl {
 
 constexpr int kBatchThreads = 512;  // C * L / 16 for every item
 
-template <class F>
-__global__ void __launch_bounds__(kBatchThreads, 2) batch_kernel(const TileArgs<F> *__restrict__ args,
+template <class F, int MINB = 2>
+__global__ void __launch_bounds__(kBatchThreads, MINB) batch_kernel(const TileArgs<F> *__restrict__ args,
                                                               const BatchItem *__restrict__ items,
                                                               unsigned long long nitems, unsigned int *counters,
                                                               BatchCtl *ctl, unsigned int spin_limit) {

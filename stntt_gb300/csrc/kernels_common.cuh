@@ -1,6 +1,7 @@
 // kernels_common.cuh -- field-generic kernels and launchers, instantiated once
 // per field by kernels_u32.cu and kernels_gl64.cu.
 #pragma once
+#include <cstdlib>
 #include <cstring>
 
 #include "batch.cuh"
@@ -140,9 +141,19 @@ void batch_args_fill_t(const PassDesc &d, uint32_t p, const void *tables, const 
     memcpy(dst, &a, sizeof(a));
 }
 
+// Blocks per SM the persistent kernel is compiled for: 2 (64 registers per
+// thread) unless STNTT_BATCH_MINB=1 selects the 128-register build.
+inline int batch_minb() {
+    static const int v = [] {
+        const char *e = getenv("STNTT_BATCH_MINB");
+        return (e && e[0] == '1') ? 1 : 2;
+    }();
+    return v;
+}
+
 template <class F>
 cudaError_t batch_prepare_t(size_t smem, int *blocks_per_sm) {
-    auto kern = batch_kernel<F>;
+    auto kern = batch_minb() == 1 ? batch_kernel<F, 1> : batch_kernel<F, 2>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     if (e != cudaSuccess)
         return e;
@@ -152,9 +163,10 @@ cudaError_t batch_prepare_t(size_t smem, int *blocks_per_sm) {
 template <class F>
 cudaError_t batch_launch_t(const void *args, const void *items, unsigned long long nitems, unsigned int *counters,
                            void *ctl, size_t smem, unsigned grid, unsigned spin_limit, cudaStream_t s) {
-    batch_kernel<F><<<grid, kBatchThreads, smem, s>>>(static_cast<const TileArgs<F> *>(args),
-                                                       static_cast<const BatchItem *>(items), nitems, counters,
-                                                       static_cast<BatchCtl *>(ctl), spin_limit);
+    auto kern = batch_minb() == 1 ? batch_kernel<F, 1> : batch_kernel<F, 2>;
+    kern<<<grid, kBatchThreads, smem, s>>>(static_cast<const TileArgs<F> *>(args),
+                                           static_cast<const BatchItem *>(items), nitems, counters,
+                                           static_cast<BatchCtl *>(ctl), spin_limit);
     return cudaGetLastError();
 }
 

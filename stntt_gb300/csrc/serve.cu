@@ -310,7 +310,7 @@ int stntt_server_create(stntt_ctx *ctx, const stntt_server_config *cfg, stntt_se
     if (cfg)
         c = *cfg;
     if (c.streams == 0)
-        c.streams = 16;
+        c.streams = 32;
     if (c.max_log_n == 0)
         c.max_log_n = 22;
     if (c.streams > 128 || c.max_log_n > 26)
