@@ -77,6 +77,8 @@ def lib():
         _bind(L, "orc_polymul_u32", None, [_u32p, sz, _u32p, sz, u32, _u32p])
         _bind(L, "orc_polymul_gl64", None, [_u64p, sz, _u64p, sz, _u64p])
         _bind(L, "orc_fnv1a64", u64, [C.c_void_p, sz])
+        _bind(L, "orc_dft_point_u32", u32, [_u32p, u64, u32, u32, u64])
+        _bind(L, "orc_dft_point_gl64", u64, [_u64p, u64, u64, u64])
         _lib = L
     return _lib
 

@@ -610,6 +610,26 @@ void orc_dft_gl64(const uint64_t *in, uint64_t *out, uint32_t n, uint64_t root) 
     }
 }
 
+uint32_t orc_dft_point_u32(const uint32_t *in, uint64_t n, uint32_t root, uint32_t mod, uint64_t k) {
+    const uint64_t wk = orc_pow_mod(root, k % n, mod);
+    uint64_t acc = 0, w = 1;
+    for (uint64_t j = 0; j < n; ++j) {
+        acc = (acc + (uint64_t)in[j] % mod * w) % mod;
+        w = w * wk % mod;
+    }
+    return (uint32_t)acc;
+}
+
+uint64_t orc_dft_point_gl64(const uint64_t *in, uint64_t n, uint64_t root, uint64_t k) {
+    const uint64_t wk = orc_gl_pow(root, k % n);
+    uint64_t acc = 0, w = 1;
+    for (uint64_t j = 0; j < n; ++j) {
+        acc = gl_add(acc, orc_gl_mul(in[j] % ORC_GL_P, w));
+        w = orc_gl_mul(w, wk);
+    }
+    return acc;
+}
+
 void orc_polymul_u32(const uint32_t *a, size_t na, const uint32_t *b, size_t nb, uint32_t mod, uint32_t *out) {
     if (!na || !nb)
         return;

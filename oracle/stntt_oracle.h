@@ -70,6 +70,10 @@ int orc_intt_gs_u32(uint32_t *vec, uint32_t n, uint32_t root, uint32_t mod);
 /* ---- schoolbook references ------------------------------------------------ */
 void orc_dft_u32(const uint32_t *in, uint32_t *out, uint32_t n, uint32_t root, uint32_t mod);
 void orc_dft_gl64(const uint64_t *in, uint64_t *out, uint32_t n, uint64_t root);
+/* One DFT output X[k] = sum_j in[j] root^(j k), O(n): spot checks at sizes
+ * where the full oracle is slow. */
+uint32_t orc_dft_point_u32(const uint32_t *in, uint64_t n, uint32_t root, uint32_t mod, uint64_t k);
+uint64_t orc_dft_point_gl64(const uint64_t *in, uint64_t n, uint64_t root, uint64_t k);
 /* out[0..na+nb-2] = a * b (linear convolution mod p). */
 void orc_polymul_u32(const uint32_t *a, size_t na, const uint32_t *b, size_t nb, uint32_t mod, uint32_t *out);
 void orc_polymul_gl64(const uint64_t *a, size_t na, const uint64_t *b, size_t nb, uint64_t *out);

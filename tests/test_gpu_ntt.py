@@ -360,3 +360,55 @@ def test_u32_primes_above_2e30(ctx, lg):
     if lg <= 10:
         want = O.polymul_u32(a[:h], b[:h], p)
         assert np.array_equal(host32(out)[: want.size], want)
+
+
+
+def _gl_add(a, b):
+    """(a + b) mod p for canonical uint64 arrays, with wrap-around arithmetic."""
+    with np.errstate(over="ignore"):
+        s = a + b
+        wrap = (s < a) | (s >= np.uint64(O.GL_P))
+        return np.where(wrap, s - np.uint64(O.GL_P), s)
+
+
+def test_largest_sizes_three_pass(ctx):
+    """Goldilocks 2^26 and the 32-bit prime 2^27 (p = 2013265921 >= 2^30: the
+    strict-reduction kernels), both three HBM passes: spot DFT values from the
+    oracle, linearity, round trip."""
+    for field, lg in (("gl64", 26), ("u32", 27)):
+        n = 1 << lg
+        if field == "gl64":
+            x, y = O.uniform_u64(71, n), O.uniform_u64(72, n)
+            d, dy = dev64(x), dev64(y)
+            ctx.ntt_gl64(d, lg)
+            ctx.ntt_gl64(dy, lg)
+            f, fy = host64(d), host64(dy)
+            root = O.gl_root(lg)
+            for k in (0, 1, 777, n - 1):
+                assert int(f[k]) == O.lib().orc_dft_point_gl64(x, n, root, k), (field, k)
+            # linearity on the transform of x + y
+            ds = dev64(_gl_add(x, y))
+            ctx.ntt_gl64(ds, lg)
+            assert np.array_equal(host64(ds), _gl_add(f, fy))
+            ctx.ntt_gl64(d, lg, inverse=True)
+            assert np.array_equal(host64(d), x)
+        else:
+            p, root = st.params_u32(lg)
+            assert p == 2013265921
+            x = O.uniform_u32(73, p, n)
+            d = dev32(x)
+            ctx.ntt_u32(d, lg, 1, p, root)
+            f = host32(d)
+            for k in (0, 1, 777, n - 1):
+                assert int(f[k]) == O.lib().orc_dft_point_u32(x, n, root, p, k), (field, k)
+            ctx.ntt_u32(d, lg, 1, p, root, inverse=True)
+            assert np.array_equal(host32(d), x)
+
+
+def test_empty_and_null_arguments(ctx):
+    p, root = st.params_u32(10)
+    assert st.lib().stntt_ntt_u32(ctx.handle, None, 10, 0, p, root, 0, 0, None) == 0  # empty batch: no-op
+    assert st.lib().stntt_ntt_gl64(ctx.handle, None, 10, 0, 0, None) == 0
+    assert st.lib().stntt_ntt_u32(ctx.handle, None, 10, 1, p, root, 0, 0, None) == 1  # null data: EINVAL
+    assert st.lib().stntt_ntt_gl64(ctx.handle, None, 10, 1, 0, None) == 1
+    assert st.lib().stntt_ntt_batch(ctx.handle, None, 0, None) == 0

@@ -140,3 +140,16 @@ def test_gl_mul_reduction_equals_remainder():
     for a in vals:
         for b in vals[:40]:
             assert L.orc_gl_mul(a % O.GL_P, b % O.GL_P) == L.orc_gl_mul_slow(a, b) == (a * b) % O.GL_P
+
+
+def test_dft_point_matches_full_dft():
+    for lg in (3, 7, 9):
+        n = 1 << lg
+        root, p = O.find_params(n, 11)
+        x = O.uniform_u32(lg, p, n)
+        full = O.dft_u32(x, root, p)
+        y = O.uniform_u64(lg, n)
+        fg = O.dft_gl64(y, O.gl_root(lg))
+        for k in (0, 1, n // 3, n - 1):
+            assert O.lib().orc_dft_point_u32(x, n, root, p, k) == full[k]
+            assert O.lib().orc_dft_point_gl64(y, n, O.gl_root(lg), k) == fg[k]
