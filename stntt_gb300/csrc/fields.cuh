@@ -76,20 +76,19 @@ struct FieldGL {
     uint32_t p;  // unused; keeps the two field types interchangeable
 
     __device__ __forceinline__ T add(T a, T b) const {
-        // s = a + b; if (carry or s >= p) s = s + (2^32 - 1) mod 2^64.
+        // a + b = a - (p - b): p - b lies in [1, p], so the subtraction below
+        // (one conditional + p on borrow) returns a canonical value. Seven
+        // integer ops against nine for an add with a carry fix and a compare.
         uint32_t s0, s1;
         asm("{\n\t"
-            ".reg .u32 c, d, x0, x1;\n\t"
-            ".reg .pred q;\n\t"
-            "add.cc.u32 %0, %2, %4;\n\t"
-            "addc.cc.u32 %1, %3, %5;\n\t"
-            "addc.u32 c, 0, 0;\n\t"
-            "add.cc.u32 x0, %0, 0xffffffff;\n\t"
-            "addc.cc.u32 x1, %1, 0;\n\t"
-            "addc.u32 d, c, 0;\n\t"
-            "setp.ne.u32 q, d, 0;\n\t"
-            "selp.u32 %0, x0, %0, q;\n\t"
-            "selp.u32 %1, x1, %1, q;\n\t"
+            ".reg .u32 n0, n1, m;\n\t"
+            "sub.cc.u32 n0, 1, %4;\n\t"
+            "subc.u32 n1, 0xffffffff, %5;\n\t"
+            "sub.cc.u32 %0, %2, n0;\n\t"
+            "subc.cc.u32 %1, %3, n1;\n\t"
+            "subc.u32 m, 0, 0;\n\t"
+            "sub.cc.u32 %0, %0, m;\n\t"
+            "subc.u32 %1, %1, 0;\n\t"
             "}"
             : "=&r"(s0), "=&r"(s1)
             : "r"((uint32_t)a), "r"((uint32_t)(a >> 32)), "r"((uint32_t)b), "r"((uint32_t)(b >> 32)));
@@ -115,8 +114,7 @@ struct FieldGL {
     __device__ __forceinline__ T mul(T a, T b) const {
         uint32_t r0, r1;
         asm("{\n\t"
-            ".reg .u32 r2, r3, t0, t1, m, u0, u1, c, x0, x1, d;\n\t"
-            ".reg .pred q;\n\t"
+            ".reg .u32 r2, r3, t0, t1, m, u0, u1;\n\t"
             // 128-bit product (r3:r2:r1:r0) = a * b
             "mul.lo.u32 %0, %2, %4;\n\t"
             "mul.hi.u32 %1, %2, %4;\n\t"
@@ -127,29 +125,24 @@ struct FieldGL {
             "madc.hi.u32 r3, %3, %5, 0;\n\t"
             "mad.lo.cc.u32 r2, %3, %5, r2;\n\t"
             "addc.u32 r3, r3, 0;\n\t"
-            // t = (r1:r0) - r3; on borrow t -= 2^32 - 1
+            // t = (r1:r0) - r3; on borrow add p (i.e. subtract 2^32 - 1)
             "sub.cc.u32 t0, %0, r3;\n\t"
             "subc.cc.u32 t1, %1, 0;\n\t"
             "subc.u32 m, 0, 0;\n\t"
             "sub.cc.u32 t0, t0, m;\n\t"
             "subc.u32 t1, t1, 0;\n\t"
-            // u = r2 * (2^32 - 1) = (r2 << 32) - r2
-            "sub.cc.u32 u0, 0, r2;\n\t"
-            "subc.u32 u1, r2, 0;\n\t"
-            // s = t + u; on carry s += 2^32 - 1 (cannot carry again)
-            "add.cc.u32 t0, t0, u0;\n\t"
-            "addc.cc.u32 t1, t1, u1;\n\t"
-            "addc.u32 c, 0, 0;\n\t"
-            "neg.s32 c, c;\n\t"
-            "add.cc.u32 t0, t0, c;\n\t"
-            "addc.u32 t1, t1, 0;\n\t"
-            // canonical: if s >= p then s -= p (s + 2^32 - 1 carries out)
-            "add.cc.u32 x0, t0, 0xffffffff;\n\t"
-            "addc.cc.u32 x1, t1, 0;\n\t"
-            "addc.u32 d, 0, 0;\n\t"
-            "setp.ne.u32 q, d, 0;\n\t"
-            "selp.u32 %0, x0, t0, q;\n\t"
-            "selp.u32 %1, x1, t1, q;\n\t"
+            // u = r2 * (2^32 - 1) <= (2^32 - 1)^2; result = t + u = t - (p - u).
+            // p - u = (~r2 + k) * 2^32 + (r2 + 1), k the carry of r2 + 1; both
+            // limbs as multiply-adds (r2 * 1 + 1, r2 * (2^32 - 1) + 2^32 - 1 = ~r2),
+            // which run on the FMA pipe beside the ALU-bound carry chains.
+            "mad.lo.cc.u32 u0, r2, 1, 1;\n\t"
+            "madc.lo.u32 u1, r2, 0xffffffff, 0xffffffff;\n\t"
+            // t + u < 2p, so one conditional + p on borrow leaves it canonical
+            "sub.cc.u32 %0, t0, u0;\n\t"
+            "subc.cc.u32 %1, t1, u1;\n\t"
+            "subc.u32 m, 0, 0;\n\t"
+            "sub.cc.u32 %0, %0, m;\n\t"
+            "subc.u32 %1, %1, 0;\n\t"
             "}"
             : "=&r"(r0), "=&r"(r1)
             : "r"((uint32_t)a), "r"((uint32_t)(a >> 32)), "r"((uint32_t)b), "r"((uint32_t)(b >> 32)));

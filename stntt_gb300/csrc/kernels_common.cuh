@@ -17,9 +17,9 @@ __device__ __forceinline__ typename F::TW to_tw(uint64_t raw) {
     return w;
 }
 
-template <class F, int E, int TAIL, bool IN2 = false>
-cudaError_t launch_tile_e(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks, cudaStream_t s) {
-    auto kern = tile_kernel<F, E, TAIL, IN2>;
+// Launch one tile kernel, raising its dynamic shared-memory limit once per device.
+template <class F, auto KERN>
+cudaError_t launch_tile_k(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks, cudaStream_t s) {
     static bool attr_set[64] = {};  // per device: the opt-in shared-memory size of this kernel
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -28,15 +28,39 @@ cudaError_t launch_tile_e(const PassDesc &d, const TileArgs<F> &a, uint64_t bloc
     if (dev < 0 || dev >= 64)
         return cudaErrorInvalidDevice;
     if (!attr_set[dev]) {
-        e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        e = cudaFuncSetAttribute(KERN, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         if (e != cudaSuccess)
             return e;
         attr_set[dev] = true;
     }
     if (d.smem_bytes > 200 * 1024)
         return cudaErrorInvalidConfiguration;
-    kern<<<(unsigned)blocks, d.threads, d.smem_bytes, s>>>(a);
+    KERN<<<(unsigned)blocks, d.threads, d.smem_bytes, s>>>(a);
     return cudaGetLastError();
+}
+
+template <class F, int E, int TAIL, bool IN2 = false>
+cudaError_t launch_tile_e(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks, cudaStream_t s) {
+    return launch_tile_k<F, tile_kernel<F, E, TAIL, IN2>>(d, a, blocks, s);
+}
+
+// Tile lengths 2^4..2^13 at 16 elements per thread: the kernel with the
+// length compiled in. false when logL is outside that range.
+template <class F>
+bool launch_tile_fixed(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks, cudaStream_t s, cudaError_t *e) {
+    switch (d.logL) {
+    case 4: *e = launch_tile_k<F, tile_kernel_l<F, 4>>(d, a, blocks, s); return true;
+    case 5: *e = launch_tile_k<F, tile_kernel_l<F, 5>>(d, a, blocks, s); return true;
+    case 6: *e = launch_tile_k<F, tile_kernel_l<F, 6>>(d, a, blocks, s); return true;
+    case 7: *e = launch_tile_k<F, tile_kernel_l<F, 7>>(d, a, blocks, s); return true;
+    case 8: *e = launch_tile_k<F, tile_kernel_l<F, 8>>(d, a, blocks, s); return true;
+    case 9: *e = launch_tile_k<F, tile_kernel_l<F, 9>>(d, a, blocks, s); return true;
+    case 10: *e = launch_tile_k<F, tile_kernel_l<F, 10>>(d, a, blocks, s); return true;
+    case 11: *e = launch_tile_k<F, tile_kernel_l<F, 11>>(d, a, blocks, s); return true;
+    case 12: *e = launch_tile_k<F, tile_kernel_l<F, 12>>(d, a, blocks, s); return true;
+    case 13: *e = launch_tile_k<F, tile_kernel_l<F, 13>>(d, a, blocks, s); return true;
+    default: return false;
+    }
 }
 
 template <class F>
@@ -100,6 +124,9 @@ cudaError_t launch_tile_t(const PassDesc &d, uint32_t p, const void *tables, con
         default: return cudaErrorNotSupported;
         }
     }
+    cudaError_t e;
+    if (d.E == 16 && launch_tile_fixed<F>(d, a, blocks, s, &e))
+        return e;
     switch (d.E) {
     case 2: return launch_tile_e<F, 2, 1>(d, a, blocks, s);
     case 4: return launch_tile_e<F, 4, 2>(d, a, blocks, s);

@@ -60,14 +60,17 @@ template <class F>
 struct Pad;
 template <>
 struct Pad<FieldU32> {
+    static constexpr uint32_t PS = 5;
     static __device__ __forceinline__ uint32_t at(uint32_t i) { return i + (i >> 5); }
 };
 template <>
 struct Pad<FieldU32L> {
+    static constexpr uint32_t PS = 5;
     static __device__ __forceinline__ uint32_t at(uint32_t i) { return i + (i >> 5); }
 };
 template <>
 struct Pad<FieldGL> {
+    static constexpr uint32_t PS = 4;
     static __device__ __forceinline__ uint32_t at(uint32_t i) { return i + (i >> 4); }
 };
 
@@ -90,11 +93,9 @@ __device__ __forceinline__ void dft_reg(const F &f, typename F::T *x, const type
 #pragma unroll
             for (int j = 0; j < h; ++j) {
                 const typename F::T a = x[base + j], b = x[base + j + h];
+                const typename F::T d = j == 0 ? f.sub(a, b) : f.sub_lazy(a, b);
                 x[base + j] = f.add(a, b);
-                if (j == 0)
-                    x[base + j + h] = f.sub(a, b);
-                else
-                    x[base + j + h] = f.mul_tw(f.sub_lazy(a, b), w16[j * (16 / (2 * h))]);
+                x[base + j + h] = j == 0 ? d : f.mul_tw(d, w16[j * (16 / (2 * h))]);
             }
         }
     }
@@ -108,6 +109,24 @@ struct Geo {
     uint64_t istride, ostride, col;
     bool valid;  // false for the padding rows of a partial last CTA
 };
+
+// Output k = pos of a tile's last step: the four-step twiddle w_M^(col * pos)
+// (COL) or n^-1 (ROW with do_scale), then the canonical value to HBM.
+template <class F>
+__device__ __forceinline__ void store_last(const TileArgs<F> &a, const F &f, const Geo<typename F::T> &g,
+                                           uint32_t pos, typename F::T v) {
+    if (a.mode == kModeCol) {
+        const uint64_t e = g.col * pos;
+        const uint32_t lo = (uint32_t)(e & ((1ull << a.h) - 1));
+        const uint32_t hi = (uint32_t)(e >> a.h);
+        v = f.mul_tw(f.mul_tw(v, __ldg(&a.tw4_lo[lo])), __ldg(&a.tw4_hi[hi]));
+    } else if (a.do_scale) {
+        v = f.mul_tw(v, a.scale);
+    }
+    v = f.canon(v);
+    if (g.valid)
+        g.dst[(uint64_t)pos * g.ostride] = v;
+}
 
 template <class F, int E, int LOGR, bool first, bool last, bool in2 = false>
 __device__ __forceinline__ void tile_step(const TileArgs<F> &a, const F &f, typename F::T (&x)[E],
@@ -163,17 +182,7 @@ __device__ __forceinline__ void tile_step(const TileArgs<F> &a, const F &f, type
             const uint32_t pos = base + ((uint32_t)r << logp);
             T v = x[m * R + bit_reverse<LOGR>(r)];
             if constexpr (last) {
-                if (a.mode == kModeCol) {
-                    const uint64_t e = g.col * pos;
-                    const uint32_t lo = (uint32_t)(e & ((1ull << a.h) - 1));
-                    const uint32_t hi = (uint32_t)(e >> a.h);
-                    v = f.mul_tw(f.mul_tw(v, __ldg(&a.tw4_lo[lo])), __ldg(&a.tw4_hi[hi]));
-                } else if (a.do_scale) {
-                    v = f.mul_tw(v, a.scale);
-                }
-                v = f.canon(v);
-                if (g.valid)
-                    g.dst[(uint64_t)pos * g.ostride] = v;
+                store_last(a, f, g, pos, v);
             } else {
                 col_sm[Pad<F>::at(pos)] = v;
             }
@@ -208,19 +217,15 @@ __device__ __forceinline__ bool first_step(const TileArgs<F> &a, const F &f, typ
     return false;
 }
 
-// One CTA's worth of work: C columns (COL) or rows (ROW) with global index
-// blk * C + c over the batch. Used by tile_kernel (blk = blockIdx.x) and by
-// the persistent batched kernel (blk from its work list).
-template <class F, int E, int TAIL, bool IN2 = false>
-__device__ __forceinline__ void tile_run(const TileArgs<F> &a, uint64_t blk, typename F::T *sm) {
+// Which column (COL) or row (ROW) thread threadIdx.x works on, its index u
+// within it, and the HBM addresses of its first and last step.
+template <class F, int E>
+__device__ __forceinline__ Geo<typename F::T> tile_geo(const TileArgs<F> &a, uint64_t blk, uint32_t &c,
+                                                       uint32_t &u) {
     using T = typename F::T;
-    F f;
-    f.p = a.p;
-
     const uint32_t C = 1u << a.logC;
     constexpr uint32_t logE = E >= 32 ? 5 : E >= 16 ? 4 : E >= 8 ? 3 : E >= 4 ? 2 : 1;
     const uint32_t logU = a.logL - logE;  // log2(L / E): threads per column
-    uint32_t c, u;
     if (a.tfast) {
         u = threadIdx.x & ((1u << logU) - 1);
         c = threadIdx.x >> logU;
@@ -261,6 +266,20 @@ __device__ __forceinline__ void tile_run(const TileArgs<F> &a, uint64_t blk, typ
         g.dst = obase + rem;
         g.ostride = 1ull << logPer;
     }
+    return g;
+}
+
+// One CTA's worth of work: C columns (COL) or rows (ROW) with global index
+// blk * C + c over the batch. Used by tile_kernel (blk = blockIdx.x) and by
+// the persistent batched kernel (blk from its work list).
+template <class F, int E, int TAIL, bool IN2 = false>
+__device__ __forceinline__ void tile_run(const TileArgs<F> &a, uint64_t blk, typename F::T *sm) {
+    using T = typename F::T;
+    F f;
+    f.p = a.p;
+
+    uint32_t c, u;
+    const Geo<T> g = tile_geo<F, E>(a, blk, c, u);
 
     T x[E];
     const int n16 = (int)(a.logL >> 2);  // radix-16 steps after the optional leading step
@@ -282,6 +301,95 @@ template <class F, int E, int TAIL, bool IN2 = false>
 __global__ void __launch_bounds__(E >= 32 ? 512 : 1024) tile_kernel(const TileArgs<F> a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     tile_run<F, E, TAIL, IN2>(a, blockIdx.x, reinterpret_cast<typename F::T *>(smem_raw));
+}
+
+// ---- Tile length fixed at compile time -----------------------------------
+// The same Stockham steps with L = 2^LOGL a template parameter and 16
+// elements per thread: each step's stride, twiddle shift and output spacing
+// are constants, so shared-memory indices are a per-thread padded base plus
+// an immediate. The padding never separates an access from its base:
+// Pad(b + d) = Pad(b) + d + (d >> PS) for every read (b = u, d = m U + r L/R)
+// and every write (b = the item's output base, d = r p) of these steps.
+template <class F, int E, int LOGL, int LOGR, int LOGP, bool first, bool last>
+__device__ __forceinline__ void tile_step_l(const TileArgs<F> &a, const F &f, typename F::T (&x)[E],
+                                            typename F::T *col_sm, uint32_t u, const Geo<typename F::T> &g) {
+    using T = typename F::T;
+    constexpr int R = 1 << LOGR, ITEMS = E / R;
+    constexpr uint32_t PS = Pad<F>::PS, U = (1u << LOGL) / E, TS = (1u << LOGL) >> LOGR, P = 1u << LOGP;
+    static_assert(LOGR + LOGP <= LOGL, "step beyond the tile");
+    // ---- read R inputs per item: idx = u + m U + r L/R
+    const uint32_t pu = Pad<F>::at(u);
+#pragma unroll
+    for (int m = 0; m < ITEMS; ++m) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const uint32_t d = m * U + r * TS;
+            if constexpr (first)
+                x[m * R + r] = g.valid ? g.src[(uint64_t)(u + d) * g.istride] : T(0);
+            else
+                x[m * R + r] = col_sm[pu + d + (d >> PS)];
+        }
+    }
+    // ---- twiddle w_(R p)^(r k), k = t mod p, then the R-point DFT
+#pragma unroll
+    for (int m = 0; m < ITEMS; ++m) {
+        if constexpr (!first) {
+            const uint32_t k = (u + m * U) & (P - 1);
+#pragma unroll
+            for (int r = 1; r < R; ++r)
+                x[m * R + r] = f.mul_tw(x[m * R + r], __ldg(&a.twL[(r * k) << (LOGL - LOGR - LOGP)]));
+        }
+        dft_reg<F, R>(f, &x[m * R], a.wR);
+    }
+    if constexpr (!first && !last)
+        __syncthreads();  // every read of this step precedes any write
+    // ---- write output r of item t to (t - k) R + k + r p
+#pragma unroll
+    for (int m = 0; m < ITEMS; ++m) {
+        const uint32_t t = u + m * U;
+        const uint32_t k = t & (P - 1);
+        const uint32_t base = ((t - k) << LOGR) + k;
+        const uint32_t pb = Pad<F>::at(base);
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const uint32_t d = (uint32_t)r << LOGP;
+            const T v = x[m * R + bit_reverse<LOGR>(r)];
+            if constexpr (last)
+                store_last(a, f, g, base + d, v);
+            else
+                col_sm[pb + d + (d >> PS)] = v;
+        }
+    }
+    if constexpr (!last)
+        __syncthreads();
+}
+
+// Steps S.. of a 2^LOGL tile: one leading radix-2^(LOGL mod 4) step when LOGL
+// is not a multiple of 4, then radix-16 steps.
+template <class F, int E, int LOGL, int S>
+__device__ __forceinline__ void tile_steps_l(const TileArgs<F> &a, const F &f, typename F::T (&x)[E],
+                                             typename F::T *col_sm, uint32_t u, const Geo<typename F::T> &g) {
+    constexpr int TAIL = LOGL & 3;
+    constexpr int NS = (LOGL >> 2) + (TAIL > 0 ? 1 : 0);
+    if constexpr (S < NS) {
+        constexpr int LOGR = (S == 0 && TAIL > 0) ? TAIL : 4;
+        constexpr int LOGP = S == 0 ? 0 : (TAIL > 0 ? TAIL + 4 * (S - 1) : 4 * S);
+        tile_step_l<F, E, LOGL, LOGR, LOGP, S == 0, S == NS - 1>(a, f, x, col_sm, u, g);
+        tile_steps_l<F, E, LOGL, S + 1>(a, f, x, col_sm, u, g);
+    }
+}
+
+template <class F, int LOGL>
+__global__ void __launch_bounds__(1024) tile_kernel_l(const TileArgs<F> a) {
+    static_assert(LOGL >= 4, "16 elements per thread need L >= 16");
+    using T = typename F::T;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    F f;
+    f.p = a.p;
+    uint32_t c, u;
+    const Geo<T> g = tile_geo<F, 16>(a, blockIdx.x, c, u);
+    T x[16];
+    tile_steps_l<F, 16, LOGL, 0>(a, f, x, reinterpret_cast<T *>(smem_raw) + c * a.cs, u, g);
 }
 
 }  // namespace stntt

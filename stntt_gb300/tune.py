@@ -60,7 +60,7 @@ def candidates(field: int, log_n: int, full: bool = False) -> Iterable[tuple[lis
                 if len(logs) == 1:
                     per_pass.append([0])
                 else:
-                    cs = [c for c in (2, 4, 8, 16) if c * L <= (1 << 15)]
+                    cs = [c for c in (1, 2, 4, 8, 16) if c * L <= (1 << 15)]
                     per_pass.append(cs if full else cs[:3])
             for combo in itertools.product(*per_pass):
                 yield logs, [e] * len(logs), list(combo)
