@@ -44,6 +44,9 @@ cudaError_t fill_uniform_gl64(void *, size_t, uint64_t, cudaStream_t);
 cudaError_t copy_scale_u32(const void *, void *, size_t, uint64_t, uint32_t, cudaStream_t);
 cudaError_t copy_scale_gl64(const void *, void *, size_t, uint64_t, cudaStream_t);
 cudaError_t launch_gl_probe(uint64_t *, unsigned, int, cudaStream_t);
+cudaError_t preload_u32();
+cudaError_t preload_u32l();
+cudaError_t preload_gl64();
 size_t batch_args_size_u32();
 size_t batch_args_size_gl64();
 void batch_args_fill_u32(const PassDesc &, uint32_t, const void *, const unsigned long long *,
@@ -78,6 +81,15 @@ uint64_t host_tw_entry(int field, uint64_t w, uint32_t p) {
         return w;
     const uint64_t wp = (w << 32) / p;  // Shoup companion floor(w * 2^32 / p)
     return (w & 0xffffffffull) | (wp << 32);
+}
+
+cudaError_t preload_kernels() {
+    cudaError_t e = preload_u32();
+    if (e == cudaSuccess)
+        e = preload_u32l();
+    if (e == cudaSuccess)
+        e = preload_gl64();
+    return e;
 }
 
 cudaError_t launch_tile(int field, const PassDesc &d, uint32_t p, const void *tables, const void *in, void *out,
@@ -649,6 +661,15 @@ int stntt_init(stntt_ctx **out, int device) {
         cudaStreamCreateWithFlags(&ctx->host_stream, cudaStreamNonBlocking) != cudaSuccess) {
         if (ctx->setup)
             cudaStreamDestroy(ctx->setup);
+        delete ctx;
+        return STNTT_ECUDA;
+    }
+    // Load every kernel now: a lazy load at first use would stall the device
+    // in the middle of a caller's stream of work. This also fails early when
+    // the library holds no code for this GPU.
+    if (preload_kernels() != cudaSuccess) {
+        cudaStreamDestroy(ctx->setup);
+        cudaStreamDestroy(ctx->host_stream);
         delete ctx;
         return STNTT_ECUDA;
     }

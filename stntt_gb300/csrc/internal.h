@@ -40,6 +40,10 @@ cudaError_t launch_stage_u32(const void *in, void *out, const void *tw, uint32_t
 cudaError_t launch_copy_scale(int field, const void *in, void *out, size_t count, uint64_t scale_tw, uint32_t p,
                               cudaStream_t s);
 
+// Load every kernel of the library on the current device (see
+// preload_tiles_t); run once per device when a context is created.
+cudaError_t preload_kernels();
+
 // Host modular helpers
 uint64_t host_pow_mod(uint64_t b, uint64_t e, uint64_t m);
 uint64_t host_gl_mul(uint64_t a, uint64_t b);

@@ -3,6 +3,7 @@
 #pragma once
 #include <cstdlib>
 #include <cstring>
+#include <utility>
 
 #include "batch.cuh"
 #include "internal.h"
@@ -17,10 +18,11 @@ __device__ __forceinline__ typename F::TW to_tw(uint64_t raw) {
     return w;
 }
 
-// Launch one tile kernel, raising its dynamic shared-memory limit once per device.
+// Raise one tile kernel's dynamic shared-memory limit, once per device. The
+// call also loads the kernel's code, so the first launch does not.
 template <class F, auto KERN>
-cudaError_t launch_tile_k(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks, cudaStream_t s) {
-    static bool attr_set[64] = {};  // per device: the opt-in shared-memory size of this kernel
+cudaError_t tile_attr() {
+    static bool attr_set[64] = {};  // per device
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess)
@@ -33,10 +35,23 @@ cudaError_t launch_tile_k(const PassDesc &d, const TileArgs<F> &a, uint64_t bloc
             return e;
         attr_set[dev] = true;
     }
+    return cudaSuccess;
+}
+
+template <class F, auto KERN>
+cudaError_t launch_tile_k(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks, cudaStream_t s) {
+    cudaError_t e = tile_attr<F, KERN>();
+    if (e != cudaSuccess)
+        return e;
     if (d.smem_bytes > 200 * 1024)
         return cudaErrorInvalidConfiguration;
     KERN<<<(unsigned)blocks, d.threads, d.smem_bytes, s>>>(a);
     return cudaGetLastError();
+}
+
+template <class F, int LOGL>
+cudaError_t launch_tile_l(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks, cudaStream_t s) {
+    return launch_tile_k<F, tile_kernel_l<F, LOGL>>(d, a, blocks, s);
 }
 
 template <class F, int E, int TAIL, bool IN2 = false>
@@ -49,16 +64,16 @@ cudaError_t launch_tile_e(const PassDesc &d, const TileArgs<F> &a, uint64_t bloc
 template <class F>
 bool launch_tile_fixed(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks, cudaStream_t s, cudaError_t *e) {
     switch (d.logL) {
-    case 4: *e = launch_tile_k<F, tile_kernel_l<F, 4>>(d, a, blocks, s); return true;
-    case 5: *e = launch_tile_k<F, tile_kernel_l<F, 5>>(d, a, blocks, s); return true;
-    case 6: *e = launch_tile_k<F, tile_kernel_l<F, 6>>(d, a, blocks, s); return true;
-    case 7: *e = launch_tile_k<F, tile_kernel_l<F, 7>>(d, a, blocks, s); return true;
-    case 8: *e = launch_tile_k<F, tile_kernel_l<F, 8>>(d, a, blocks, s); return true;
-    case 9: *e = launch_tile_k<F, tile_kernel_l<F, 9>>(d, a, blocks, s); return true;
-    case 10: *e = launch_tile_k<F, tile_kernel_l<F, 10>>(d, a, blocks, s); return true;
-    case 11: *e = launch_tile_k<F, tile_kernel_l<F, 11>>(d, a, blocks, s); return true;
-    case 12: *e = launch_tile_k<F, tile_kernel_l<F, 12>>(d, a, blocks, s); return true;
-    case 13: *e = launch_tile_k<F, tile_kernel_l<F, 13>>(d, a, blocks, s); return true;
+    case 4: *e = launch_tile_l<F, 4>(d, a, blocks, s); return true;
+    case 5: *e = launch_tile_l<F, 5>(d, a, blocks, s); return true;
+    case 6: *e = launch_tile_l<F, 6>(d, a, blocks, s); return true;
+    case 7: *e = launch_tile_l<F, 7>(d, a, blocks, s); return true;
+    case 8: *e = launch_tile_l<F, 8>(d, a, blocks, s); return true;
+    case 9: *e = launch_tile_l<F, 9>(d, a, blocks, s); return true;
+    case 10: *e = launch_tile_l<F, 10>(d, a, blocks, s); return true;
+    case 11: *e = launch_tile_l<F, 11>(d, a, blocks, s); return true;
+    case 12: *e = launch_tile_l<F, 12>(d, a, blocks, s); return true;
+    case 13: *e = launch_tile_l<F, 13>(d, a, blocks, s); return true;
     default: return false;
     }
 }
@@ -195,6 +210,37 @@ cudaError_t batch_launch_t(const void *args, const void *items, unsigned long lo
                                            static_cast<const BatchItem *>(items), nitems, counters,
                                            static_cast<BatchCtl *>(ctl), spin_limit);
     return cudaGetLastError();
+}
+
+// Load every tile and batch kernel of a field on the current device (CUDA
+// loads kernel code lazily, at first use; a load in the middle of a serving
+// loop stalls the device for a while), and set their shared-memory limits.
+template <class F, int... LOGL>
+cudaError_t preload_fixed_t(std::integer_sequence<int, LOGL...>) {
+    cudaError_t e = cudaSuccess;
+    ((e = (e == cudaSuccess ? tile_attr<F, tile_kernel_l<F, LOGL + 4>>() : e)), ...);
+    return e;
+}
+
+template <class F>
+cudaError_t preload_tiles_t() {
+    const cudaError_t list[] = {
+        tile_attr<F, tile_kernel<F, 2, 1>>(),        tile_attr<F, tile_kernel<F, 4, 2>>(),
+        tile_attr<F, tile_kernel<F, 8, 3>>(),        tile_attr<F, tile_kernel<F, 16, 0>>(),
+        tile_attr<F, tile_kernel<F, 16, 1>>(),       tile_attr<F, tile_kernel<F, 16, 2>>(),
+        tile_attr<F, tile_kernel<F, 16, 3>>(),       tile_attr<F, tile_kernel<F, 32, 0>>(),
+        tile_attr<F, tile_kernel<F, 32, 1>>(),       tile_attr<F, tile_kernel<F, 32, 2>>(),
+        tile_attr<F, tile_kernel<F, 32, 3>>(),       tile_attr<F, tile_kernel<F, 2, 1, true>>(),
+        tile_attr<F, tile_kernel<F, 4, 2, true>>(),  tile_attr<F, tile_kernel<F, 8, 3, true>>(),
+        tile_attr<F, tile_kernel<F, 16, 0, true>>(), tile_attr<F, tile_kernel<F, 16, 1, true>>(),
+        tile_attr<F, tile_kernel<F, 16, 2, true>>(), tile_attr<F, tile_kernel<F, 16, 3, true>>(),
+        preload_fixed_t<F>(std::make_integer_sequence<int, 10>{}),
+    };
+    for (cudaError_t e : list)
+        if (e != cudaSuccess)
+            return e;
+    int blocks = 0;
+    return batch_prepare_t<F>(0, &blocks);
 }
 
 // out[i] = scale * base^i as twiddle entries

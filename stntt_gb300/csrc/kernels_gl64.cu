@@ -125,4 +125,18 @@ cudaError_t launch_gl_probe(uint64_t *out, unsigned blocks, int reps, cudaStream
     return cudaGetLastError();
 }
 
+cudaError_t preload_gl64() {
+    cudaFuncAttributes at;
+    cudaError_t e = preload_tiles_t<FieldGL>();
+    if (e == cudaSuccess)
+        e = cudaFuncGetAttributes(&at, gen_powers_kernel<FieldGL>);
+    if (e == cudaSuccess)
+        e = cudaFuncGetAttributes(&at, pointwise_kernel<FieldGL>);
+    if (e == cudaSuccess)
+        e = cudaFuncGetAttributes(&at, copy_scale_kernel<FieldGL>);
+    if (e == cudaSuccess)
+        e = cudaFuncGetAttributes(&at, fill_uniform_gl64_kernel);
+    return e;
+}
+
 }  // namespace stntt

@@ -125,4 +125,20 @@ cudaError_t batch_launch_u32(const void *args, const void *items, unsigned long 
     return batch_launch_t<FieldU32>(args, items, nitems, counters, ctl, smem, grid, spin_limit, s);
 }
 
+cudaError_t preload_u32() {
+    cudaFuncAttributes at;
+    cudaError_t e = preload_tiles_t<FieldU32>();
+    if (e == cudaSuccess)
+        e = cudaFuncGetAttributes(&at, stage_u32_kernel);
+    if (e == cudaSuccess)
+        e = cudaFuncGetAttributes(&at, gen_powers_kernel<FieldU32>);
+    if (e == cudaSuccess)
+        e = cudaFuncGetAttributes(&at, pointwise_kernel<FieldU32>);
+    if (e == cudaSuccess)
+        e = cudaFuncGetAttributes(&at, copy_scale_kernel<FieldU32>);
+    if (e == cudaSuccess)
+        e = cudaFuncGetAttributes(&at, fill_uniform_u32_kernel);
+    return e;
+}
+
 }  // namespace stntt

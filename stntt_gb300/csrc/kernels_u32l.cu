@@ -15,4 +15,6 @@ cudaError_t batch_launch_u32l(const void *args, const void *items, unsigned long
     return batch_launch_t<FieldU32L>(args, items, nitems, counters, ctl, smem, grid, spin_limit, s);
 }
 
+cudaError_t preload_u32l() { return preload_tiles_t<FieldU32L>(); }
+
 }  // namespace stntt

@@ -45,7 +45,8 @@ def splits(log_n: int, max_pass: int = 13) -> list[list[int]]:
 
 
 def candidates(field: int, log_n: int, full: bool = False) -> Iterable[tuple[list[int], list[int], list[int]]]:
-    """Plan shapes to try. Without `full`, only even-ish splits are kept."""
+    """Plan shapes to try: every columns-per-CTA choice; without `full`, only the
+    three most even two-pass splits and the most even three-pass split."""
     sp = splits(log_n)
     if not full:
         two = sorted([s for s in sp if len(s) <= 2], key=lambda s: max(s) - min(s))[:3]
@@ -61,7 +62,7 @@ def candidates(field: int, log_n: int, full: bool = False) -> Iterable[tuple[lis
                     per_pass.append([0])
                 else:
                     cs = [c for c in (1, 2, 4, 8, 16) if c * L <= (1 << 15)]
-                    per_pass.append(cs if full else cs[:3])
+                    per_pass.append(cs)
             for combo in itertools.product(*per_pass):
                 yield logs, [e] * len(logs), list(combo)
 
