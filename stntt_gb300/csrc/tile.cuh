@@ -103,10 +103,11 @@ __device__ __forceinline__ void dft_reg(const F &f, typename F::T *x, const type
 
 template <class T>
 struct Geo {
-    const T *src;   // element j of this column/row: src[j * istride]
+    const T *src;   // element j of this column/row
     const T *src2;  // second input for the fused pointwise product, or null
-    T *dst;        // element k: dst[k * ostride]
-    uint64_t istride, ostride, col;
+    T *dst;        // element k of the output
+    uint32_t istride, ostride;  // element j at src[j * istride], k at dst[k * ostride] (< 2^32)
+    uint32_t col;             // COL: column index within the sub-problem (< 2^28)
     bool valid;  // false for the padding rows of a partial last CTA
 };
 
@@ -116,7 +117,7 @@ template <class F>
 __device__ __forceinline__ void store_last(const TileArgs<F> &a, const F &f, const Geo<typename F::T> &g,
                                            uint32_t pos, typename F::T v) {
     if (a.mode == kModeCol) {
-        const uint64_t e = g.col * pos;
+        const uint64_t e = (uint64_t)g.col * pos;
         const uint32_t lo = (uint32_t)(e & ((1ull << a.h) - 1));
         const uint32_t hi = (uint32_t)(e >> a.h);
         v = f.mul_tw(f.mul_tw(v, __ldg(&a.tw4_lo[lo])), __ldg(&a.tw4_hi[hi]));
@@ -250,12 +251,12 @@ __device__ __forceinline__ Geo<typename F::T> tile_geo(const TileArgs<F> &a, uin
     g.src2 = nullptr;
     if (a.mode == kModeCol) {
         const uint64_t q = rem >> a.logS;
-        g.col = rem & ((1ull << a.logS) - 1);
+        g.col = (uint32_t)(rem & ((1ull << a.logS) - 1));
         g.src = ibase + (q << a.logM) + g.col;
         if (ibase2)
             g.src2 = ibase2 + (q << a.logM) + g.col;
         g.dst = obase + (q << a.logM) + g.col;
-        g.istride = g.ostride = 1ull << a.logS;
+        g.istride = g.ostride = 1u << a.logS;
     } else {
         const uint64_t inrow = ((rem & ((1ull << a.logN1) - 1)) << a.logN2) + (rem >> a.logN1);
         g.col = 0;
@@ -264,7 +265,7 @@ __device__ __forceinline__ Geo<typename F::T> tile_geo(const TileArgs<F> &a, uin
             g.src2 = ibase2 + (inrow << a.logL);
         g.istride = 1;
         g.dst = obase + rem;
-        g.ostride = 1ull << logPer;
+        g.ostride = 1u << logPer;
     }
     return g;
 }
