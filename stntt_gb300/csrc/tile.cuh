@@ -380,17 +380,24 @@ __device__ __forceinline__ void tile_steps_l(const TileArgs<F> &a, const F &f, t
     }
 }
 
+// One CTA's worth of work with the tile length compiled in (the counterpart
+// of tile_run for 16 elements per thread).
 template <class F, int LOGL>
-__global__ void __launch_bounds__(1024) tile_kernel_l(const TileArgs<F> a) {
+__device__ __forceinline__ void tile_run_l(const TileArgs<F> &a, uint64_t blk, typename F::T *sm) {
     static_assert(LOGL >= 4, "16 elements per thread need L >= 16");
     using T = typename F::T;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
     F f;
     f.p = a.p;
     uint32_t c, u;
-    const Geo<T> g = tile_geo<F, 16>(a, blockIdx.x, c, u);
+    const Geo<T> g = tile_geo<F, 16>(a, blk, c, u);
     T x[16];
-    tile_steps_l<F, 16, LOGL, 0>(a, f, x, reinterpret_cast<T *>(smem_raw) + c * a.cs, u, g);
+    tile_steps_l<F, 16, LOGL, 0>(a, f, x, sm + c * a.cs, u, g);
+}
+
+template <class F, int LOGL>
+__global__ void __launch_bounds__(1024) tile_kernel_l(const TileArgs<F> a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    tile_run_l<F, LOGL>(a, blockIdx.x, reinterpret_cast<typename F::T *>(smem_raw));
 }
 
 }  // namespace stntt
