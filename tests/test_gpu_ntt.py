@@ -412,3 +412,44 @@ def test_empty_and_null_arguments(ctx):
     assert st.lib().stntt_ntt_u32(ctx.handle, None, 10, 1, p, root, 0, 0, None) == 1  # null data: EINVAL
     assert st.lib().stntt_ntt_gl64(ctx.handle, None, 10, 1, 0, None) == 1
     assert st.lib().stntt_ntt_batch(ctx.handle, None, 0, None) == 0
+
+
+def test_single_transforms_in_a_cuda_graph(ctx):
+    """The device calls are capturable: forward + inverse captured once per
+    size on a side stream (after a warm-up call on it builds the plan and its
+    workspace), replayed; results equal the oracle and the round trip."""
+    s = torch.cuda.Stream()
+    for field, lg in (("u32", 16), ("gl64", 20), ("u32", 13)):
+        n = 1 << lg
+        if field == "gl64":
+            x = O.uniform_u64(90 + lg, n)
+            d = dev64(x)
+            fwd = lambda: ctx.ntt_gl64(d, lg, stream=s.cuda_stream)  # noqa: E731
+            inv = lambda: ctx.ntt_gl64(d, lg, inverse=True, stream=s.cuda_stream)  # noqa: E731
+            want, host = O.ntt_gl64(x), host64
+        else:
+            p, root = st.params_u32(lg)
+            x = O.uniform_u32(90 + lg, p, n)
+            d = dev32(x)
+            fwd = lambda: ctx.ntt_u32(d, lg, 1, p, root, stream=s.cuda_stream)  # noqa: E731
+            inv = lambda: ctx.ntt_u32(d, lg, 1, p, root, inverse=True, stream=s.cuda_stream)  # noqa: E731
+            want, host = O.ntt_u32(x, root, p), host32
+        torch.cuda.synchronize()
+        with torch.cuda.stream(s):
+            fwd()
+            inv()
+        torch.cuda.synchronize()
+        gf, gi = torch.cuda.CUDAGraph(), torch.cuda.CUDAGraph()
+        with torch.cuda.graph(gf, stream=s, capture_error_mode="relaxed"):
+            fwd()
+        with torch.cuda.graph(gi, stream=s, capture_error_mode="relaxed"):
+            inv()
+        with torch.cuda.stream(s):
+            gf.replay()
+        assert np.array_equal(host(d), want), (field, lg)
+        with torch.cuda.stream(s):
+            gi.replay()
+            for _ in range(3):
+                gf.replay()
+                gi.replay()
+        assert np.array_equal(host(d), x), (field, lg)
