@@ -35,6 +35,14 @@ struct BatchCtl {
 
 constexpr int kBatchThreads = 512;  // C * L / 16 for every item
 
+// One work item with the tile length compiled in, as a called function: its
+// registers are allocated on their own, not together with the other lengths'
+// bodies and the persistent loop around them.
+template <class F, int LOGL>
+__device__ __noinline__ void batch_item_l(const TileArgs<F> &a, uint64_t blk, typename F::T *sm) {
+    tile_run_l<F, LOGL>(a, blk, sm);
+}
+
 template <class F, int MINB = 2>
 __global__ void __launch_bounds__(kBatchThreads, MINB) batch_kernel(const TileArgs<F> *__restrict__ args,
                                                               const BatchItem *__restrict__ items,
@@ -74,11 +82,24 @@ __global__ void __launch_bounds__(kBatchThreads, MINB) batch_kernel(const TileAr
         }
         __syncthreads();
         if (s_ok) {
-            switch (sa.logL & 3) {
-            case 0: tile_run<F, 16, 0>(sa, bi.blk, sm); break;
-            case 1: tile_run<F, 16, 1>(sa, bi.blk, sm); break;
-            case 2: tile_run<F, 16, 2>(sa, bi.blk, sm); break;
-            default: tile_run<F, 16, 3>(sa, bi.blk, sm); break;
+            switch (sa.logL) {  // every item: 16 elements per thread
+            case 4: batch_item_l<F, 4>(sa, bi.blk, sm); break;
+            case 5: batch_item_l<F, 5>(sa, bi.blk, sm); break;
+            case 6: batch_item_l<F, 6>(sa, bi.blk, sm); break;
+            case 7: batch_item_l<F, 7>(sa, bi.blk, sm); break;
+            case 8: batch_item_l<F, 8>(sa, bi.blk, sm); break;
+            case 9: batch_item_l<F, 9>(sa, bi.blk, sm); break;
+            case 10: batch_item_l<F, 10>(sa, bi.blk, sm); break;
+            case 11: batch_item_l<F, 11>(sa, bi.blk, sm); break;
+            case 12: batch_item_l<F, 12>(sa, bi.blk, sm); break;
+            case 13: batch_item_l<F, 13>(sa, bi.blk, sm); break;
+            default:
+                switch (sa.logL & 3) {
+                case 0: tile_run<F, 16, 0>(sa, bi.blk, sm); break;
+                case 1: tile_run<F, 16, 1>(sa, bi.blk, sm); break;
+                case 2: tile_run<F, 16, 2>(sa, bi.blk, sm); break;
+                default: tile_run<F, 16, 3>(sa, bi.blk, sm); break;
+                }
             }
         }
         __threadfence();  // this item's stores before the signal below
