@@ -258,6 +258,26 @@ uint64_t fmul(int field, uint64_t a, uint64_t b, uint32_t p) {
     return field == kFieldGL ? host_gl_mul(a, b) : (uint64_t)((u128)a * b % p);
 }
 
+// Shared-memory stride between a CTA's columns (elements): the padded length
+// rounded up to a residue, modulo the bank count (16 eight-byte or 32
+// four-byte banks), that spreads one warp access over the banks. Threads
+// running along a column (tfast): U threads per column, residue U. Threads
+// across columns: C columns side by side, residue banks / C; from C = banks
+// up every thread of a phase reads the same row of C different columns, so
+// the residue must be odd. (A simulation of every step's accesses chose these;
+// an even stride there made all C columns hit one bank.)
+uint32_t column_stride(int field, uint32_t L, uint32_t C, uint32_t U, uint32_t tfast) {
+    const uint32_t padshift = field == kFieldGL ? 4 : 5;
+    const uint32_t banks = field == kFieldGL ? 16 : 32;
+    const uint32_t base = L + (L >> padshift);
+    uint32_t want;
+    if (tfast)
+        want = U < banks ? U : 0;
+    else
+        want = C < banks ? banks / C : 1;
+    return base + ((want + banks - base % banks) % banks);
+}
+
 // Tile geometry for one pass: elements per thread E, columns per CTA C,
 // shared-memory column stride and size.
 void shape_pass(PassDesc &d, int field, uint64_t col_limit, uint32_t want_E, uint32_t want_C) {
@@ -287,15 +307,7 @@ void shape_pass(PassDesc &d, int field, uint64_t col_limit, uint32_t want_E, uin
         C >>= 1;
     d.logC = ilog2(C);
     d.threads = (uint32_t)(C * U);
-    const uint32_t padshift = field == kFieldGL ? 4 : 5;
-    const uint32_t banks = field == kFieldGL ? 16 : 32;
-    const uint32_t base = L + (L >> padshift);
-    uint32_t want;
-    if (d.tfast)
-        want = U < banks ? U : 0;
-    else
-        want = C < banks ? (uint32_t)(banks / C) : 0;
-    d.cs = base + ((want + banks - base % banks) % banks);
+    d.cs = column_stride(field, L, (uint32_t)C, U, d.tfast);
     d.smem_bytes = (size_t)C * d.cs * (field == kFieldGL ? 8 : 4);
 }
 
@@ -1260,10 +1272,7 @@ void batch_shape(PassDesc &d, int field) {
     const uint32_t U = L / 16, C = 8192 / L;
     d.logC = ilog2(C);
     d.threads = C * U;
-    const uint32_t padshift = field == kFieldGL ? 4 : 5, banks = field == kFieldGL ? 16 : 32;
-    const uint32_t base = L + (L >> padshift);
-    const uint32_t want = d.tfast ? (U < banks ? U : 0) : (C < banks ? banks / C : 0);
-    d.cs = base + ((want + banks - base % banks) % banks);
+    d.cs = column_stride(field, L, C, U, d.tfast);
     d.smem_bytes = (size_t)C * d.cs * (field == kFieldGL ? 8 : 4);
 }
 

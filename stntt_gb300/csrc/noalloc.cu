@@ -81,7 +81,8 @@ void shape(PassDesc &d, uint64_t col_limit) {
     d.logC = lg2(C);
     d.threads = (uint32_t)(C * U);
     const uint32_t banks = 16, base = L + (L >> 4);
-    const uint32_t want = d.tfast ? (U < banks ? U : 0) : (C < banks ? (uint32_t)(banks / C) : 0);
+    // odd stride from C = banks up: each phase reads one row of C columns
+    const uint32_t want = d.tfast ? (U < banks ? U : 0) : (C < banks ? (uint32_t)(banks / C) : 1);
     d.cs = base + ((want + banks - base % banks) % banks);
     d.smem_bytes = (size_t)C * d.cs * 8;
 }
