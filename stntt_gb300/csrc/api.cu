@@ -36,6 +36,10 @@ cudaError_t batch_launch_u32l(const void *, const void *, unsigned long long, un
 cudaError_t launch_tile_gl64(const PassDesc &, uint32_t, const void *, const void *, void *, uint64_t, cudaStream_t,
                              const void *);
 cudaError_t gen_powers_u32(void *, uint64_t, uint64_t, uint64_t, uint32_t, cudaStream_t);
+cudaError_t gen_four_step_u32(void *, const void *, const void *, uint32_t, uint32_t, uint64_t, uint32_t,
+                               cudaStream_t);
+cudaError_t gen_four_step_gl64(void *, const void *, const void *, uint32_t, uint32_t, uint64_t, uint32_t,
+                                cudaStream_t);
 cudaError_t gen_powers_gl64(void *, uint64_t, uint64_t, uint64_t, cudaStream_t);
 cudaError_t pointwise_u32(const void *, const void *, void *, size_t, uint32_t, cudaStream_t);
 cudaError_t pointwise_gl64(const void *, const void *, void *, size_t, cudaStream_t);
@@ -104,6 +108,11 @@ cudaError_t launch_gen_powers(int field, void *out, uint64_t count, uint64_t bas
                               cudaStream_t s) {
     return field == kFieldGL ? gen_powers_gl64(out, count, base, scale, s)
                              : gen_powers_u32(out, count, base, scale, p, s);
+}
+cudaError_t launch_gen_four_step(int field, void *out, const void *lo, const void *hi, uint32_t h, uint32_t logS,
+                                 uint64_t count, uint32_t p, cudaStream_t s) {
+    return field == kFieldGL ? gen_four_step_gl64(out, lo, hi, h, logS, count, p, s)
+                             : gen_four_step_u32(out, lo, hi, h, logS, count, p, s);
 }
 cudaError_t launch_pointwise(int field, const void *a, const void *b, void *out, size_t count, uint32_t p,
                              cudaStream_t s) {
@@ -332,13 +341,25 @@ int build_plan(stntt_ctx *ctx, Plan &pl, int field, uint32_t log_n, uint32_t p, 
             logs.push_back(log_n / K + (i < log_n % K ? 1 : 0));
     }
     const uint32_t K = (uint32_t)logs.size();
+    // Tables, generated in this order into one allocation: powers (count,
+    // base, scale), or a column pass's full four-step table (built from its
+    // lo / hi tables, which come earlier).
     struct TableReq {
         uint64_t count, base, scale;
+        bool full;
+        uint64_t lo_off, hi_off;
+        uint32_t h, logS;
     };
     std::vector<TableReq> reqs;
     uint64_t off = 0;
     auto add_table = [&](uint64_t count, uint64_t base, uint64_t scale) {
-        reqs.push_back({count, base, scale});
+        reqs.push_back({count, base, scale, false, 0, 0, 0, 0});
+        const uint64_t o = off;
+        off += count;
+        return o;
+    };
+    auto add_full = [&](uint64_t count, uint64_t lo_off, uint64_t hi_off, uint32_t h, uint32_t logS) {
+        reqs.push_back({count, 0, 0, true, lo_off, hi_off, h, logS});
         const uint64_t o = off;
         off += count;
         return o;
@@ -373,6 +394,13 @@ int build_plan(stntt_ctx *ctx, Plan &pl, int field, uint32_t log_n, uint32_t p, 
             const uint64_t wM = fpow(field, root_dir, n >> d.logM, p);
             d.lo_off = add_table(1ull << d.h, wM, 1);
             d.hi_off = add_table(1ull << (d.logM - d.h), fpow(field, wM, 1ull << d.h, p), i == 0 ? ninv : 1);
+            // Column passes over 2^14..2^20-point sub-problems read the twiddle
+            // w_M^(col*pos) from a table laid out like the data: one load and
+            // one product per element instead of two lookups and two products
+            // (M entries per plan; the lo / hi tables stay for the kernels
+            // without this path).
+            if (d.logM >= kFullTwiddleMinLog && d.logM <= kFullTwiddleMaxLog)
+                d.full_off = add_full(1ull << d.logM, d.lo_off, d.hi_off, d.h, d.logS);
             col_limit = 1ull << d.logS;
         } else {
             d.mode = kModeRow;
@@ -394,9 +422,11 @@ int build_plan(stntt_ctx *ctx, Plan &pl, int field, uint32_t log_n, uint32_t p, 
         return cuda_fail(ctx, e, "cudaMalloc(twiddle tables)");
     }
     uint64_t o = 0;
+    char *tb = static_cast<char *>(pl.d_tables);
     for (const auto &r : reqs) {
-        e = launch_gen_powers(field, static_cast<char *>(pl.d_tables) + o * esz, r.count, r.base, r.scale, p,
-                              ctx->setup);
+        e = r.full ? launch_gen_four_step(field, tb + o * esz, tb + r.lo_off * esz, tb + r.hi_off * esz, r.h, r.logS,
+                                          r.count, p, ctx->setup)
+                   : launch_gen_powers(field, tb + o * esz, r.count, r.base, r.scale, p, ctx->setup);
         if (e != cudaSuccess)
             return cuda_fail(ctx, e, "twiddle generation launch");
         o += r.count;

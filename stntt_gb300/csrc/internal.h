@@ -10,6 +10,11 @@ namespace stntt {
 
 enum : int { kFieldU32 = 0, kFieldGL = 1 };
 enum : uint32_t { kModeCol = 0, kModeRow = 1 };  // tile pass kinds (tile.cuh)
+// Column passes over sub-problems of 2^14..2^20 points read their four-step
+// twiddle from a full table (at most 8 MB, so it stays in L2 across the
+// batch and the sub-problems); larger ones, whose table would stream from
+// HBM on the store path, keep the two-level lookup.
+constexpr uint32_t kFullTwiddleMinLog = 14, kFullTwiddleMaxLog = 20;
 
 // One HBM pass of a transform plan (see tile.cuh for the meaning of the fields).
 struct PassDesc {
@@ -19,6 +24,7 @@ struct PassDesc {
     uint32_t threads = 0;     // threads per CTA
     size_t smem_bytes = 0;
     uint64_t tw_off = 0, lo_off = 0, hi_off = 0;  // table offsets, in table entries
+    uint64_t full_off = ~0ull;  // COL: w_M^(col*pos) for every (pos, col), laid out like the data; ~0 = none
     uint64_t wR[8] = {};      // raw twiddle entries (u32: {w, w'} packed little-endian)
     uint64_t scale = 0;       // raw twiddle entry
 };
@@ -29,6 +35,10 @@ cudaError_t launch_tile(int field, const PassDesc &d, uint32_t p, const void *ta
 // out[i] = scale * base^i, i < count, as twiddle entries (u32: Shoup pairs).
 cudaError_t launch_gen_powers(int field, void *out, uint64_t count, uint64_t base, uint64_t scale, uint32_t p,
                               cudaStream_t s);
+// out[pos * 2^logS + col] = w_M^(col * pos) for count = M entries, from the
+// two-level tables lo (w_M^e, e < 2^h) and hi (s * w_M^(e 2^h)).
+cudaError_t launch_gen_four_step(int field, void *out, const void *lo, const void *hi, uint32_t h, uint32_t logS,
+                                 uint64_t count, uint32_t p, cudaStream_t s);
 cudaError_t launch_pointwise(int field, const void *a, const void *b, void *out, size_t count, uint32_t p,
                              cudaStream_t s);
 cudaError_t launch_fill_uniform(int field, void *out, size_t count, uint64_t seed, uint32_t p, cudaStream_t s);

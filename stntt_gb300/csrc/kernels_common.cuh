@@ -49,10 +49,6 @@ cudaError_t launch_tile_k(const PassDesc &d, const TileArgs<F> &a, uint64_t bloc
     return cudaGetLastError();
 }
 
-template <class F, int LOGL>
-cudaError_t launch_tile_l(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks, cudaStream_t s) {
-    return launch_tile_k<F, tile_kernel_l<F, LOGL>>(d, a, blocks, s);
-}
 
 template <class F, int E, int TAIL, bool IN2 = false>
 cudaError_t launch_tile_e(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks, cudaStream_t s) {
@@ -60,7 +56,17 @@ cudaError_t launch_tile_e(const PassDesc &d, const TileArgs<F> &a, uint64_t bloc
 }
 
 // Tile lengths 2^4..2^13 at 16 elements per thread: the kernel with the
-// length compiled in. false when logL is outside that range.
+// length compiled in (column passes with a full four-step table from 2^6 up:
+// the FULL4 build). false when logL is outside that range.
+template <class F, int LOGL>
+cudaError_t launch_tile_l(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks, cudaStream_t s) {
+    if constexpr (LOGL >= 6) {
+        if (a.tw4_full && a.mode == kModeCol)
+            return launch_tile_k<F, tile_kernel_l<F, LOGL, true>>(d, a, blocks, s);
+    }
+    return launch_tile_k<F, tile_kernel_l<F, LOGL>>(d, a, blocks, s);
+}
+
 template <class F>
 bool launch_tile_fixed(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks, cudaStream_t s, cudaError_t *e) {
     switch (d.logL) {
@@ -88,6 +94,7 @@ void fill_args(TileArgs<F> &a, const PassDesc &d, uint32_t p, const void *tables
     a.twL = tab + d.tw_off;
     a.tw4_lo = tab + d.lo_off;
     a.tw4_hi = tab + d.hi_off;
+    a.tw4_full = d.full_off == ~0ull ? nullptr : tab + d.full_off;
     for (int j = 0; j < 8; ++j)
         std::memcpy(&a.wR[j], &d.wR[j], sizeof(TW));
     std::memcpy(&a.scale, &d.scale, sizeof(TW));
@@ -219,6 +226,8 @@ template <class F, int... LOGL>
 cudaError_t preload_fixed_t(std::integer_sequence<int, LOGL...>) {
     cudaError_t e = cudaSuccess;
     ((e = (e == cudaSuccess ? tile_attr<F, tile_kernel_l<F, LOGL + 4>>() : e)), ...);
+    ((e = (e == cudaSuccess && LOGL + 4 >= 6 ? tile_attr<F, tile_kernel_l<F, LOGL + 4, (LOGL + 4 >= 6)>>() : e)),
+     ...);
     return e;
 }
 
@@ -241,6 +250,52 @@ cudaError_t preload_tiles_t() {
             return e;
     int blocks = 0;
     return batch_prepare_t<F>(0, &blocks);
+}
+
+// Twiddle entry from a residue (u32: Shoup pair {w, floor(w 2^32 / p)}).
+template <class F>
+__device__ __forceinline__ typename F::TW make_tw(uint64_t w, uint32_t p);
+template <>
+__device__ __forceinline__ uint2 make_tw<FieldU32>(uint64_t w, uint32_t p) {
+    return make_uint2((uint32_t)w, (uint32_t)((w << 32) / p));
+}
+template <>
+__device__ __forceinline__ uint64_t make_tw<FieldGL>(uint64_t w, uint32_t) {
+    return w;
+}
+
+// The four-step twiddle of a column pass for every element of a sub-problem,
+// in the data's own layout: out[pos * S + col] = lo[e mod 2^h] * hi[e >> h],
+// e = col * pos < M.
+template <class F>
+__global__ void gen_four_step_kernel(typename F::TW *out, const typename F::TW *lo, const typename F::TW *hi,
+                                     uint32_t h, uint32_t logS, uint64_t count, uint32_t p) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count)
+        return;
+    const uint64_t e = (i >> logS) * (i & ((1ull << logS) - 1));
+    const uint64_t a = F::tw_value(lo[e & ((1ull << h) - 1)]), b = F::tw_value(hi[e >> h]);
+    uint64_t w;
+    if constexpr (sizeof(typename F::T) == 8) {
+        F f;
+        f.p = p;
+        w = f.mul(a, b);
+    } else {
+        w = a * b % p;
+    }
+    out[i] = make_tw<F>(w, p);
+}
+
+template <class F>
+cudaError_t gen_four_step_t(void *out, const void *lo, const void *hi, uint32_t h, uint32_t logS, uint64_t count,
+                            uint32_t p, cudaStream_t s) {
+    using TW = typename F::TW;
+    const uint64_t blocks = (count + 255) / 256;
+    if (!blocks)
+        return cudaSuccess;
+    gen_four_step_kernel<F><<<(unsigned)blocks, 256, 0, s>>>(static_cast<TW *>(out), static_cast<const TW *>(lo),
+                                                             static_cast<const TW *>(hi), h, logS, count, p);
+    return cudaGetLastError();
 }
 
 // out[i] = scale * base^i as twiddle entries

@@ -131,12 +131,19 @@ cudaError_t preload_gl64() {
     if (e == cudaSuccess)
         e = cudaFuncGetAttributes(&at, gen_powers_kernel<FieldGL>);
     if (e == cudaSuccess)
+        e = cudaFuncGetAttributes(&at, gen_four_step_kernel<FieldGL>);
+    if (e == cudaSuccess)
         e = cudaFuncGetAttributes(&at, pointwise_kernel<FieldGL>);
     if (e == cudaSuccess)
         e = cudaFuncGetAttributes(&at, copy_scale_kernel<FieldGL>);
     if (e == cudaSuccess)
         e = cudaFuncGetAttributes(&at, fill_uniform_gl64_kernel);
     return e;
+}
+
+cudaError_t gen_four_step_gl64(void *out, const void *lo, const void *hi, uint32_t h, uint32_t logS, uint64_t count,
+                           uint32_t p, cudaStream_t s) {
+    return gen_four_step_t<FieldGL>(out, lo, hi, h, logS, count, p, s);
 }
 
 }  // namespace stntt

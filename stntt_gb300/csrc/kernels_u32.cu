@@ -133,12 +133,19 @@ cudaError_t preload_u32() {
     if (e == cudaSuccess)
         e = cudaFuncGetAttributes(&at, gen_powers_kernel<FieldU32>);
     if (e == cudaSuccess)
+        e = cudaFuncGetAttributes(&at, gen_four_step_kernel<FieldU32>);
+    if (e == cudaSuccess)
         e = cudaFuncGetAttributes(&at, pointwise_kernel<FieldU32>);
     if (e == cudaSuccess)
         e = cudaFuncGetAttributes(&at, copy_scale_kernel<FieldU32>);
     if (e == cudaSuccess)
         e = cudaFuncGetAttributes(&at, fill_uniform_u32_kernel);
     return e;
+}
+
+cudaError_t gen_four_step_u32(void *out, const void *lo, const void *hi, uint32_t h, uint32_t logS, uint64_t count,
+                           uint32_t p, cudaStream_t s) {
+    return gen_four_step_t<FieldU32>(out, lo, hi, h, logS, count, p, s);
 }
 
 }  // namespace stntt

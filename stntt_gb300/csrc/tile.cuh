@@ -38,6 +38,7 @@ struct TileArgs {
     const TW *twL;     // w_L^e, e < L
     const TW *tw4_lo;  // COL: w_M^e, e < 2^h
     const TW *tw4_hi;  // COL: s * w_M^(e * 2^h), e < M / 2^h  (s = n^-1 on the first inverse pass)
+    const TW *tw4_full;  // COL, optional: lo * hi for every (pos, col), at pos * S + col
     TW wR[8];          // w_16^j (for L < 16: entry j*16/L holds w_L^j)
     TW scale;          // ROW with do_scale: n^-1
     uint32_t p;
@@ -112,11 +113,14 @@ struct Geo {
 };
 
 // Output k = pos of a tile's last step: the four-step twiddle w_M^(col * pos)
-// (COL) or n^-1 (ROW with do_scale), then the canonical value to HBM.
-template <class F>
+// (COL; one entry of the full table with FULL4, else the product of two
+// table entries) or n^-1 (ROW with do_scale), then the canonical value to HBM.
+template <class F, bool FULL4 = false>
 __device__ __forceinline__ void store_last(const TileArgs<F> &a, const F &f, const Geo<typename F::T> &g,
                                            uint32_t pos, typename F::T v) {
-    if (a.mode == kModeCol) {
+    if (FULL4 && a.mode == kModeCol) {
+        v = f.mul_tw(v, __ldg(&a.tw4_full[(uint64_t)pos * g.ostride + g.col]));
+    } else if (a.mode == kModeCol) {
         const uint64_t e = (uint64_t)g.col * pos;
         const uint32_t lo = (uint32_t)(e & ((1ull << a.h) - 1));
         const uint32_t hi = (uint32_t)(e >> a.h);
@@ -311,7 +315,7 @@ __global__ void __launch_bounds__(E >= 32 ? 512 : 1024) tile_kernel(const TileAr
 // an immediate. The padding never separates an access from its base:
 // Pad(b + d) = Pad(b) + d + (d >> PS) for every read (b = u, d = m U + r L/R)
 // and every write (b = the item's output base, d = r p) of these steps.
-template <class F, int E, int LOGL, int LOGR, int LOGP, bool first, bool last>
+template <class F, int E, int LOGL, int LOGR, int LOGP, bool first, bool last, bool FULL4>
 __device__ __forceinline__ void tile_step_l(const TileArgs<F> &a, const F &f, typename F::T (&x)[E],
                                             typename F::T *col_sm, uint32_t u, const Geo<typename F::T> &g) {
     using T = typename F::T;
@@ -356,7 +360,7 @@ __device__ __forceinline__ void tile_step_l(const TileArgs<F> &a, const F &f, ty
             const uint32_t d = (uint32_t)r << LOGP;
             const T v = x[m * R + bit_reverse<LOGR>(r)];
             if constexpr (last)
-                store_last(a, f, g, base + d, v);
+                store_last<F, FULL4>(a, f, g, base + d, v);
             else
                 col_sm[pb + d + (d >> PS)] = v;
         }
@@ -367,7 +371,7 @@ __device__ __forceinline__ void tile_step_l(const TileArgs<F> &a, const F &f, ty
 
 // Steps S.. of a 2^LOGL tile: one leading radix-2^(LOGL mod 4) step when LOGL
 // is not a multiple of 4, then radix-16 steps.
-template <class F, int E, int LOGL, int S>
+template <class F, int E, int LOGL, int S, bool FULL4>
 __device__ __forceinline__ void tile_steps_l(const TileArgs<F> &a, const F &f, typename F::T (&x)[E],
                                              typename F::T *col_sm, uint32_t u, const Geo<typename F::T> &g) {
     constexpr int TAIL = LOGL & 3;
@@ -375,14 +379,14 @@ __device__ __forceinline__ void tile_steps_l(const TileArgs<F> &a, const F &f, t
     if constexpr (S < NS) {
         constexpr int LOGR = (S == 0 && TAIL > 0) ? TAIL : 4;
         constexpr int LOGP = S == 0 ? 0 : (TAIL > 0 ? TAIL + 4 * (S - 1) : 4 * S);
-        tile_step_l<F, E, LOGL, LOGR, LOGP, S == 0, S == NS - 1>(a, f, x, col_sm, u, g);
-        tile_steps_l<F, E, LOGL, S + 1>(a, f, x, col_sm, u, g);
+        tile_step_l<F, E, LOGL, LOGR, LOGP, S == 0, S == NS - 1, FULL4>(a, f, x, col_sm, u, g);
+        tile_steps_l<F, E, LOGL, S + 1, FULL4>(a, f, x, col_sm, u, g);
     }
 }
 
 // One CTA's worth of work with the tile length compiled in (the counterpart
 // of tile_run for 16 elements per thread).
-template <class F, int LOGL>
+template <class F, int LOGL, bool FULL4 = false>
 __device__ __forceinline__ void tile_run_l(const TileArgs<F> &a, uint64_t blk, typename F::T *sm) {
     static_assert(LOGL >= 4, "16 elements per thread need L >= 16");
     using T = typename F::T;
@@ -391,13 +395,13 @@ __device__ __forceinline__ void tile_run_l(const TileArgs<F> &a, uint64_t blk, t
     uint32_t c, u;
     const Geo<T> g = tile_geo<F, 16>(a, blk, c, u);
     T x[16];
-    tile_steps_l<F, 16, LOGL, 0>(a, f, x, sm + c * a.cs, u, g);
+    tile_steps_l<F, 16, LOGL, 0, FULL4>(a, f, x, sm + c * a.cs, u, g);
 }
 
-template <class F, int LOGL>
+template <class F, int LOGL, bool FULL4 = false>
 __global__ void __launch_bounds__(1024) tile_kernel_l(const TileArgs<F> a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    tile_run_l<F, LOGL>(a, blockIdx.x, reinterpret_cast<typename F::T *>(smem_raw));
+    tile_run_l<F, LOGL, FULL4>(a, blockIdx.x, reinterpret_cast<typename F::T *>(smem_raw));
 }
 
 }  // namespace stntt
