@@ -61,7 +61,7 @@ def candidates(field: int, log_n: int, full: bool = False) -> Iterable[tuple[lis
                 if len(logs) == 1:
                     per_pass.append([0])
                 else:
-                    cs = [c for c in (1, 2, 4, 8, 16) if c * L <= (1 << 15)]
+                    cs = [c for c in (1, 2, 4, 8, 16, 32, 64) if c * L <= (1 << 15)]
                     per_pass.append(cs)
             for combo in itertools.product(*per_pass):
                 yield logs, [e] * len(logs), list(combo)
