@@ -95,6 +95,13 @@ int stntt_plan_info(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t p, uint3
  * stntt_clear_plans() restores the built-in defaults for every size. */
 int stntt_set_plan(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t npasses, const uint32_t *pass_logs,
                    const uint32_t *elems, const uint32_t *cols);
+/* The same for small calls only: transforms of this size in calls of fewer
+ * than 2^22 elements in all (batch * n), such as single requests, where the
+ * best shape fills the GPU with more, narrower tiles. Without it small calls
+ * use the plan above. No counterpart in the reference (it has one launch
+ * shape per n, src/cuda/ntt/ntt_kernel.cuh:31-39). */
+int stntt_set_plan_small(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t npasses, const uint32_t *pass_logs,
+                         const uint32_t *elems, const uint32_t *cols);
 int stntt_clear_plans(stntt_ctx *ctx);
 /* "name|SM count|driver version|compute capability" of a device: the key
  * under which tuned plans are cached. */

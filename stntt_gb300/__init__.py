@@ -95,6 +95,7 @@ _SIGS = {
     "stntt_prepare": (_int, [_vp, _int, _u32, _u32, _u32, _int]),
     "stntt_plan_info": (_int, [_vp, _int, _u32, _u32, _u32, _int, C.POINTER(_u32), C.POINTER(_u32)]),
     "stntt_set_plan": (_int, [_vp, _int, _u32, _u32, C.POINTER(_u32), C.POINTER(_u32), C.POINTER(_u32)]),
+    "stntt_set_plan_small": (_int, [_vp, _int, _u32, _u32, C.POINTER(_u32), C.POINTER(_u32), C.POINTER(_u32)]),
     "stntt_clear_plans": (_int, [_vp]),
     "stntt_device_key": (_int, [_int, C.c_char_p, _sz]),
     "stntt_ntt_u32": (_int, [_vp, _vp, _u32, _u32, _u32, _u32, _int, _u32, _vp]),
@@ -281,11 +282,13 @@ class Context:
                                      C.byref(n), logs), self._h)
         return n.value, list(logs)[: n.value]
 
-    def set_plan(self, field: int, log_n: int, pass_logs, elems=None, cols=None) -> None:
-        """Override the plan shape for one size (see stntt_set_plan)."""
+    def set_plan(self, field: int, log_n: int, pass_logs, elems=None, cols=None, small: bool = False) -> None:
+        """Override the plan shape for one size (stntt_set_plan); small=True sets
+        the shape for calls of fewer than 2^22 elements (stntt_set_plan_small)."""
         k = len(pass_logs)
         arr = lambda v: (_u32 * k)(*(v if v is not None else [0] * k))  # noqa: E731
-        _check(lib().stntt_set_plan(self._h, field, log_n, k, arr(pass_logs), arr(elems), arr(cols)), self._h)
+        fn = lib().stntt_set_plan_small if small else lib().stntt_set_plan
+        _check(fn(self._h, field, log_n, k, arr(pass_logs), arr(elems), arr(cols)), self._h)
 
     def clear_plans(self) -> None:
         _check(lib().stntt_clear_plans(self._h), self._h)

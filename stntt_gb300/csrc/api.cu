@@ -177,8 +177,9 @@ struct PlanKey {
     uint32_t log_n, p;
     uint64_t root;  // root of the direction (inverse: root^-1)
     int dir;
+    bool small;  // built from the shape set for small calls (stntt_set_plan_small)
     bool operator<(const PlanKey &o) const {
-        return std::tie(field, log_n, p, root, dir) < std::tie(o.field, o.log_n, o.p, o.root, o.dir);
+        return std::tie(field, log_n, p, root, dir, small) < std::tie(o.field, o.log_n, o.p, o.root, o.dir, o.small);
     }
 };
 
@@ -209,7 +210,7 @@ struct stntt_ctx {
     std::map<PlanKey, std::unique_ptr<Plan>> plans;
     std::map<std::tuple<uint32_t, uint32_t, uint32_t, int>, DevBuf> stage_tables;  // (log_n, p, root, wrap)
     std::map<cudaStream_t, DevBuf> workspaces;
-    std::map<std::pair<int, uint32_t>, PlanSpec> specs;  // (field, log_n) -> override
+    std::map<std::tuple<int, uint32_t, bool>, PlanSpec> specs;  // (field, log_n, small) -> override
     cudaStream_t setup = nullptr;
     // host-buffer calls: one at a time, on their own stream and staging buffer
     std::mutex host_mu;
@@ -437,10 +438,13 @@ int build_plan(stntt_ctx *ctx, Plan &pl, int field, uint32_t log_n, uint32_t p, 
     return STNTT_OK;
 }
 
-int get_plan(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t p, uint64_t root, int dir, const Plan **out) {
+int get_plan(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t p, uint64_t root, int dir, const Plan **out,
+             bool small) {
     const uint64_t rd = dir_root(field, root, p, dir);
-    PlanKey key{field, log_n, field == kFieldGL ? 0u : p, rd, dir};
     std::lock_guard<std::mutex> g(ctx->mu);
+    // a small call uses the small-call shape when one is set, else the plan of every call
+    small = small && ctx->specs.count({field, log_n, true});
+    PlanKey key{field, log_n, field == kFieldGL ? 0u : p, rd, dir, small};
     auto it = ctx->plans.find(key);
     if (it != ctx->plans.end()) {
         *out = it->second.get();
@@ -448,7 +452,7 @@ int get_plan(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t p, uint64_t roo
     }
     auto pl = std::make_unique<Plan>();
     PlanSpec spec;
-    auto sit = ctx->specs.find({field, log_n});
+    auto sit = ctx->specs.find({field, log_n, small});
     const bool has_spec = sit != ctx->specs.end();
     if (has_spec)
         spec = sit->second;
@@ -850,8 +854,10 @@ int stntt_plan_info(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t p, uint3
     return STNTT_OK;
 }
 
-int stntt_set_plan(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t npasses, const uint32_t *pass_logs,
-                   const uint32_t *elems, const uint32_t *cols) {
+namespace {
+
+int set_plan_for(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t npasses, const uint32_t *pass_logs,
+                 const uint32_t *elems, const uint32_t *cols, bool small) {
     if (!ctx || !pass_logs || npasses == 0 || npasses > 3)
         return fail(ctx, STNTT_EINVAL, "set_plan: bad arguments");
     if (field != STNTT_FIELD_U32 && field != STNTT_FIELD_GL64)
@@ -877,7 +883,7 @@ int stntt_set_plan(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t npasses, 
     DeviceGuard g(ctx->device);
     cudaDeviceSynchronize();  // plans about to be freed may be in use
     std::lock_guard<std::mutex> lk(ctx->mu);
-    ctx->specs[{f, log_n}] = s;
+    ctx->specs[{f, log_n, small}] = s;
     for (auto it = ctx->plans.begin(); it != ctx->plans.end();) {
         if (it->first.field == f && it->first.log_n == log_n) {
             if (it->second->d_tables)
@@ -889,6 +895,18 @@ int stntt_set_plan(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t npasses, 
         }
     }
     return STNTT_OK;
+}
+
+}  // namespace
+
+int stntt_set_plan(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t npasses, const uint32_t *pass_logs,
+                   const uint32_t *elems, const uint32_t *cols) {
+    return set_plan_for(ctx, field, log_n, npasses, pass_logs, elems, cols, false);
+}
+
+int stntt_set_plan_small(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t npasses, const uint32_t *pass_logs,
+                         const uint32_t *elems, const uint32_t *cols) {
+    return set_plan_for(ctx, field, log_n, npasses, pass_logs, elems, cols, true);
 }
 
 int stntt_device_key(int device, char *buf, size_t len) {
@@ -934,7 +952,7 @@ int stntt_ntt_u32_oop(stntt_ctx *ctx, const uint32_t *d_in, uint32_t *d_out, uin
         return STNTT_OK;
     DeviceGuard g(ctx->device);
     const Plan *pl;
-    rc = get_plan(ctx, kFieldU32, log_n, p, root, dir, &pl);
+    rc = get_plan(ctx, kFieldU32, log_n, p, root, dir, &pl, ((uint64_t)batch << log_n) < kSmallCallElems);
     if (rc)
         return rc;
     return run_plan(ctx, *pl, d_in, d_out, batch, (cudaStream_t)stream);
@@ -995,7 +1013,7 @@ int stntt_ntt_gl64_oop(stntt_ctx *ctx, const uint64_t *d_in, uint64_t *d_out, ui
     uint64_t r;
     stntt_gl64_root(log_n, &r);
     const Plan *pl;
-    int rc = get_plan(ctx, kFieldGL, log_n, 0, r, dir, &pl);
+    int rc = get_plan(ctx, kFieldGL, log_n, 0, r, dir, &pl, ((uint64_t)batch << log_n) < kSmallCallElems);
     if (rc)
         return rc;
     return run_plan(ctx, *pl, d_in, d_out, batch, (cudaStream_t)stream);
@@ -1141,9 +1159,10 @@ int polymul_impl(stntt_ctx *ctx, int field, const void *a, const void *b, void *
     const size_t esz = field == kFieldGL ? 8 : 4;
     const size_t bytes = ((size_t)1 << log_n) * esz;
     const Plan *fwd, *inv;
-    int rc = get_plan(ctx, field, log_n, p, root, STNTT_FORWARD, &fwd);
+    const bool small = (1ull << log_n) < kSmallCallElems;
+    int rc = get_plan(ctx, field, log_n, p, root, STNTT_FORWARD, &fwd, small);
     if (!rc)
-        rc = get_plan(ctx, field, log_n, p, root, STNTT_INVERSE, &inv);
+        rc = get_plan(ctx, field, log_n, p, root, STNTT_INVERSE, &inv, small);
     if (rc)
         return rc;
     // workspace: [pass scratch n][second operand n]

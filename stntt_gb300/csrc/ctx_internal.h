@@ -13,7 +13,11 @@ namespace sd {
 struct Plan;
 
 // Twiddle tables and pass list for one transform (built and cached on first use).
-int get_plan(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t p, uint64_t root, int dir, const Plan **out);
+// small: the call transforms fewer than kSmallCallElems elements in all (it
+// uses the small-call shape when stntt_set_plan_small set one).
+constexpr uint64_t kSmallCallElems = 1ull << 22;
+int get_plan(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t p, uint64_t root, int dir, const Plan **out,
+             bool small = false);
 // Run a plan: first pass reads `in`, last pass writes `out`, on stream s.
 // in2: optional second input whose product with `in` the first pass transforms.
 int run_plan(stntt_ctx *ctx, const Plan &pl, const void *in, void *out, uint64_t batch, cudaStream_t s,

@@ -185,7 +185,7 @@ int launch(stntt_server *sv, Slot &sl) {
         rc = sd::polymul_impl(sv->ctx, field, a, b, a, r.log_n, p, root, sl.s);
     } else {
         const sd::Plan *pl = nullptr;
-        rc = sd::get_plan(sv->ctx, field, r.log_n, p, root, (int)r.dir, &pl);
+        rc = sd::get_plan(sv->ctx, field, r.log_n, p, root, (int)r.dir, &pl, (1ull << r.log_n) < sd::kSmallCallElems);
         if (!rc)
             rc = sd::run_plan(sv->ctx, *pl, a, a, 1, sl.s);
     }

@@ -67,27 +67,34 @@ def candidates(field: int, log_n: int, full: bool = False) -> Iterable[tuple[lis
                 yield logs, [e] * len(logs), list(combo)
 
 
-def _time_plan(ctx: st.Context, field: int, log_n: int, data, p: int, root: int, batch: int, reps: int) -> float:
+def _time_plan(ctx: st.Context, field: int, log_n: int, data, p: int, root: int, batch: int, reps: int,
+               flush) -> float:
+    """Mean device time of one forward call (CUDA events around each call),
+    with L2 flushed before every call as in bench.py."""
     import torch
 
     run = (lambda: ctx.ntt_gl64(data, log_n, batch)) if field == st.FIELD_GL64 else \
         (lambda: ctx.ntt_u32(data, log_n, batch, p, root))
     run()
     torch.cuda.synchronize()
-    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    a.record()
-    for _ in range(reps):
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+    for a, b in ev:
+        flush.zero_()
+        a.record()
         run()
-    b.record()
+        b.record()
     torch.cuda.synchronize()
-    return a.elapsed_time(b) * 1e3 / reps  # microseconds per call
+    return sum(a.elapsed_time(b) for a, b in ev) * 1e3 / reps  # microseconds per call
 
 
-def tune(ctx: st.Context, field: int, log_n: int, reps: int = 10, full: bool = False, verbose: bool = False):
-    """Return (best_spec, best_us, all_results) for one size; leaves the best plan set."""
+def tune(ctx: st.Context, field: int, log_n: int, reps: int = 10, full: bool = False, verbose: bool = False,
+         batch: int = 0):
+    """Return (best_spec, best_us, all_results) for one size; leaves the best plan set.
+    batch 0: enough transforms for 2^24 elements (a GPU-filling batch)."""
     import torch
 
-    batch = max(1, (1 << 24) >> log_n)
+    batch = batch or max(1, (1 << 24) >> log_n)
+    small = (batch << log_n) < (1 << 22)  # these calls use the small-call shape
     n = batch << log_n
     if field == st.FIELD_GL64:
         data = torch.empty(n, dtype=torch.int64, device=f"cuda:{ctx.device}")
@@ -97,11 +104,12 @@ def tune(ctx: st.Context, field: int, log_n: int, reps: int = 10, full: bool = F
         p, root = st.params_u32(log_n)
         data = torch.empty(n, dtype=torch.int32, device=f"cuda:{ctx.device}")
         st.fill_uniform_u32(data, 99, p)
+    flush = torch.empty(64 << 20, dtype=torch.int32, device=f"cuda:{ctx.device}")  # 256 MiB, twice L2
     results = []
     for logs, es, cs in candidates(field, log_n, full):
         try:
-            ctx.set_plan(field, log_n, logs, es, cs)
-            us = _time_plan(ctx, field, log_n, data, p, root, batch, reps)
+            ctx.set_plan(field, log_n, logs, es, cs, small=small)
+            us = _time_plan(ctx, field, log_n, data, p, root, batch, reps, flush)
         except st.StnttError as e:
             if verbose:
                 print("skip", logs, es, cs, e)
@@ -111,7 +119,7 @@ def tune(ctx: st.Context, field: int, log_n: int, reps: int = 10, full: bool = F
             print(f"{logs} E={es} C={cs}: {us:.1f} us", flush=True)
     results.sort(key=lambda r: r["us"])
     best = results[0]
-    ctx.set_plan(field, log_n, best["logs"], best["E"], best["C"])
+    ctx.set_plan(field, log_n, best["logs"], best["E"], best["C"], small=small)
     return best, results
 
 
@@ -146,17 +154,20 @@ def apply_cache(ctx: st.Context, path: Path = DEFAULT_CACHE) -> int:
     entries.update(load_cache(path).get(key, {}))
     k = 0
     for name, e in entries.items():
-        field_s, lg = name.split(":")
-        field = st.FIELD_GL64 if field_s == "gl64" else st.FIELD_U32
-        ctx.set_plan(field, int(lg), e["logs"], e["E"], e["C"])
+        parts = name.split(":")  # "field:log_n", or "field:log_n:b1" for single-transform calls
+        field = st.FIELD_GL64 if parts[0] == "gl64" else st.FIELD_U32
+        ctx.set_plan(field, int(parts[1]), e["logs"], e["E"], e["C"], small=len(parts) > 2)
         k += 1
     return k
 
 
 def record(ctx: st.Context, field: int, log_n: int, best: dict, path: Path = DEFAULT_CACHE) -> None:
+    """Store a tuned shape; timed on single transforms that do not fill the GPU
+    (batch * n < 2^22), it is stored as the small-call shape ("...:b1")."""
     cache = load_cache(path)
     ent = cache.setdefault(_key(ctx.device), {})
-    ent[f"{'gl64' if field == st.FIELD_GL64 else 'u32'}:{log_n}"] = {
+    small = (best["batch"] << log_n) < (1 << 22)
+    ent[f"{'gl64' if field == st.FIELD_GL64 else 'u32'}:{log_n}" + (":b1" if small else "")] = {
         "logs": best["logs"], "E": best["E"], "C": best["C"], "us": best["us"], "batch": best["batch"],
         "when": time.strftime("%Y-%m-%dT%H:%M:%SZ", time.gmtime())}
     save_cache(cache, path)
@@ -179,6 +190,7 @@ def main() -> None:
     ap.add_argument("--log-n", type=int, nargs="+", default=[20, 24])
     ap.add_argument("--reps", type=int, default=10)
     ap.add_argument("--full", action="store_true")
+    ap.add_argument("--batch", type=int, default=0, help="transforms per timed call (0: 2^24 elements' worth)")
     ap.add_argument("--cache", default=str(DEFAULT_CACHE))
     ap.add_argument("--verbose", action="store_true")
     ap.add_argument("--out", default=None, help="also write all timings here (JSON)")
@@ -188,9 +200,9 @@ def main() -> None:
     ctx = st.Context(0)
     allres = {}
     for lg in args.log_n:
-        best, res = tune(ctx, field, lg, args.reps, args.full, args.verbose)
+        best, res = tune(ctx, field, lg, args.reps, args.full, args.verbose, args.batch)
         record(ctx, field, lg, best, Path(args.cache))
-        allres[f"{args.field}:{lg}"] = res
+        allres[f"{args.field}:{lg}" + (":b1" if (best["batch"] << lg) < (1 << 22) else "")] = res
         print(json.dumps({"size": f"{args.field}:{lg}", "best": best, "candidates": len(res)}), flush=True)
     if args.out:
         Path(args.out).write_text(json.dumps(allres, indent=1))

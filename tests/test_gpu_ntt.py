@@ -453,3 +453,35 @@ def test_single_transforms_in_a_cuda_graph(ctx):
                 gf.replay()
                 gi.replay()
         assert np.array_equal(host(d), x), (field, lg)
+
+
+def test_small_call_plans(ctx):
+    """stntt_set_plan_small: a separate shape for calls of fewer than 2^22
+    elements; single transforms take it, a 2^22-element batch takes the main
+    plan, and both are bit-exact."""
+    try:
+        for field, lg in (("gl64", 16), ("u32", 16)):
+            fid = st.FIELD_GL64 if field == "gl64" else st.FIELD_U32
+            ctx.set_plan(fid, lg, [6, 10], [16, 16], [8, 2], small=True)
+            ctx.set_plan(fid, lg, [9, 7], [16, 16], [4, 16])
+            for batch in (1, 64):
+                n = batch << lg
+                if field == "gl64":
+                    x = O.uniform_u64(300 + batch, n)
+                    d = dev64(x)
+                    ctx.ntt_gl64(d, lg, batch)
+                    assert np.array_equal(host64(d), O.ntt_gl64(x, batch=batch, threads=8)), (field, batch)
+                    ctx.ntt_gl64(d, lg, batch, inverse=True)
+                    assert np.array_equal(host64(d), x)
+                else:
+                    p, root = st.params_u32(lg)
+                    x = O.uniform_u32(300 + batch, p, n)
+                    d = dev32(x)
+                    ctx.ntt_u32(d, lg, batch, p, root)
+                    assert np.array_equal(host32(d), O.ntt_u32(x, root, p, batch=batch, threads=8)), (field, batch)
+                    ctx.ntt_u32(d, lg, batch, p, root, inverse=True)
+                    assert np.array_equal(host32(d), x)
+    finally:
+        ctx.clear_plans()
+        from stntt_gb300 import tune
+        tune.apply_cache(ctx)
