@@ -49,6 +49,10 @@ cudaError_t copy_scale_u32(const void *, void *, size_t, uint64_t, uint32_t, cud
 cudaError_t copy_scale_gl64(const void *, void *, size_t, uint64_t, cudaStream_t);
 cudaError_t launch_gl_probe(uint64_t *, unsigned, int, cudaStream_t);
 cudaError_t preload_u32();
+cudaError_t launch_cluster_u32l(const PassDesc &, const PassDesc &, uint32_t, const void *, const void *, void *,
+                                uint64_t, uint32_t, uint32_t, size_t, cudaStream_t);
+cudaError_t launch_cluster_gl64(const PassDesc &, const PassDesc &, uint32_t, const void *, const void *, void *,
+                                uint64_t, uint32_t, uint32_t, size_t, cudaStream_t);
 cudaError_t preload_u32l();
 cudaError_t preload_gl64();
 size_t batch_args_size_u32();
@@ -108,6 +112,15 @@ cudaError_t launch_gen_powers(int field, void *out, uint64_t count, uint64_t bas
                               cudaStream_t s) {
     return field == kFieldGL ? gen_powers_gl64(out, count, base, scale, s)
                              : gen_powers_u32(out, count, base, scale, p, s);
+}
+cudaError_t launch_cluster(int field, const PassDesc &d1, const PassDesc &d2, uint32_t p, const void *tables,
+                           const void *in, void *out, uint64_t batch, uint32_t xoff, uint32_t xs, size_t smem,
+                           cudaStream_t s) {
+    if (field == kFieldGL)
+        return launch_cluster_gl64(d1, d2, p, tables, in, out, batch, xoff, xs, smem, s);
+    if (p < (1u << 30))
+        return launch_cluster_u32l(d1, d2, p, tables, in, out, batch, xoff, xs, smem, s);
+    return cudaErrorNotSupported;
 }
 cudaError_t launch_gen_four_step(int field, void *out, const void *lo, const void *hi, uint32_t h, uint32_t logS,
                                  uint64_t count, uint32_t p, cudaStream_t s) {
@@ -517,6 +530,36 @@ int check_u32_args(stntt_ctx *ctx, uint32_t log_n, uint32_t p, uint32_t root) {
     return STNTT_OK;
 }
 
+// A two-pass plan's passes as one launch of 8-CTA clusters: CTA r takes n2/8
+// columns in the first pass and n1/8 rows in the second, exchanging through
+// distributed shared memory. STNTT_EUNSUPPORTED when the shape does not fit
+// (tile lengths 2^7..2^9 with 16 elements per thread, the shared memory of a
+// CTA, a prime without the lazy kernels).
+int run_cluster(stntt_ctx *ctx, const Plan &pl, const void *in, void *out, uint64_t batch, cudaStream_t s) {
+    const PassDesc &p1 = pl.passes[0], &p2 = pl.passes[1];
+    if (p1.E != 16 || p2.E != 16 || p1.mode != kModeCol || p2.mode != kModeRow)
+        return STNTT_EUNSUPPORTED;
+    const uint32_t L1 = p1.logL, L2 = p2.logL;
+    if (L1 < 7 || L1 > 9 || L2 < 7 || L2 > 9 || L1 + L2 < 14 || L1 + L2 > 17)
+        return STNTT_EUNSUPPORTED;
+    PassDesc d1 = p1, d2 = p2;
+    shape_pass(d1, pl.field, 1ull << p1.logS, 16, 1u << (L2 - kClusterLog));  // column limit: the sub-problem's columns
+    shape_pass(d2, pl.field, 1ull << 20, 16, 1u << (L1 - kClusterLog));
+    if (d1.logC != L2 - kClusterLog || d2.logC != L1 - kClusterLog || d1.threads != d2.threads)
+        return STNTT_EUNSUPPORTED;
+    const size_t esz = pl.field == kFieldGL ? 8 : 4;
+    const uint32_t xs = (1u << L1) + 1;  // odd: conflict-free column writes and row gathers
+    const uint64_t work = std::max<uint64_t>((uint64_t)d1.cs << d1.logC, (uint64_t)d2.cs << d2.logC);
+    const uint32_t xoff = (uint32_t)((work + 3) & ~3ull);
+    const size_t smem = (xoff + ((uint64_t)xs << d1.logC)) * esz;
+    if (smem > 200 * 1024)
+        return STNTT_EUNSUPPORTED;
+    const cudaError_t e = launch_cluster(pl.field, d1, d2, pl.p, pl.d_tables, in, out, batch, xoff, xs, smem, s);
+    if (e == cudaErrorNotSupported)
+        return STNTT_EUNSUPPORTED;
+    return e == cudaSuccess ? STNTT_OK : cuda_fail(ctx, e, "cluster launch");
+}
+
 // Run a plan: first pass reads `in`, last pass writes `out`.
 int run_plan(stntt_ctx *ctx, const Plan &pl, const void *in, void *out, uint64_t batch, cudaStream_t s,
              const void *in2) {
@@ -533,6 +576,12 @@ int run_plan(stntt_ctx *ctx, const Plan &pl, const void *in, void *out, uint64_t
                 return cuda_fail(ctx, e, "cudaMemcpyAsync");
         }
         return STNTT_OK;
+    }
+    if (!in2 && pl.passes.size() == 2 && ((uint64_t)batch << pl.log_n) < kSmallCallElems) {
+        // Small two-pass calls: both passes in one cluster launch (cluster.cuh).
+        const int rc = run_cluster(ctx, pl, in, out, batch, s);
+        if (rc != STNTT_EUNSUPPORTED)
+            return rc;
     }
     void *ws = nullptr;
     if (pl.passes.size() > 1) {

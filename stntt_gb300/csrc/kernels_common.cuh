@@ -6,6 +6,7 @@
 #include <utility>
 
 #include "batch.cuh"
+#include "cluster.cuh"
 #include "internal.h"
 #include "tile.cuh"
 
@@ -82,6 +83,32 @@ bool launch_tile_fixed(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks,
     case 13: *e = launch_tile_l<F, 13>(d, a, blocks, s); return true;
     default: return false;
     }
+}
+
+// ---- one-launch transforms in a thread-block cluster (cluster.cuh)
+template <class F, int LOG1, int LOG2>
+cudaError_t launch_cluster_k(const TileArgs<F> &a1, const TileArgs<F> &a2, uint32_t xoff, uint32_t xs,
+                             uint64_t blocks, uint32_t threads, size_t smem, cudaStream_t s) {
+    auto kern = cluster_kernel<F, LOG1, LOG2, true>;
+    cudaError_t e = tile_attr<F, cluster_kernel<F, LOG1, LOG2, true>>();
+    if (e != cudaSuccess)
+        return e;
+    if (smem > 200 * 1024 || blocks > 0x7fffffffull)
+        return cudaErrorInvalidConfiguration;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)blocks);
+    cfg.blockDim = dim3(threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 1u << kClusterLog;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelEx(&cfg, kern, a1, a2, xoff, xs);
+    return e == cudaSuccess ? cudaGetLastError() : e;
 }
 
 template <class F>
@@ -169,6 +196,49 @@ cudaError_t launch_tile_t(const PassDesc &d, uint32_t p, const void *tables, con
         }
     default: return cudaErrorInvalidValue;
     }
+}
+
+// Both passes of a two-pass plan in one cluster launch: d1 / d2 already hold
+// n2/8 columns and n1/8 rows per CTA. cudaErrorNotSupported when this split
+// (tile lengths 2^7..2^9, n = 2^14..2^17) or a missing full four-step table
+// rules it out; the caller then launches the two passes.
+template <class F>
+cudaError_t launch_cluster_t(const PassDesc &d1, const PassDesc &d2, uint32_t p, const void *tables, const void *in,
+                             void *out, uint64_t batch, uint32_t xoff, uint32_t xs, size_t smem, cudaStream_t s) {
+    TileArgs<F> a1, a2;
+    fill_args<F>(a1, d1, p, tables, in, nullptr);
+    fill_args<F>(a2, d2, p, tables, nullptr, out);
+    a1.total = batch << (d1.logN - d1.logL);
+    a2.total = batch << (d2.logN - d2.logL);
+    if (!a1.tw4_full)
+        return cudaErrorNotSupported;
+    const uint64_t blocks = batch << kClusterLog;
+    const uint32_t t = d1.threads;
+    switch (d1.logL * 16 + d2.logL) {
+    case 7 * 16 + 7: return launch_cluster_k<F, 7, 7>(a1, a2, xoff, xs, blocks, t, smem, s);
+    case 7 * 16 + 8: return launch_cluster_k<F, 7, 8>(a1, a2, xoff, xs, blocks, t, smem, s);
+    case 8 * 16 + 7: return launch_cluster_k<F, 8, 7>(a1, a2, xoff, xs, blocks, t, smem, s);
+    case 7 * 16 + 9: return launch_cluster_k<F, 7, 9>(a1, a2, xoff, xs, blocks, t, smem, s);
+    case 8 * 16 + 8: return launch_cluster_k<F, 8, 8>(a1, a2, xoff, xs, blocks, t, smem, s);
+    case 9 * 16 + 7: return launch_cluster_k<F, 9, 7>(a1, a2, xoff, xs, blocks, t, smem, s);
+    case 8 * 16 + 9: return launch_cluster_k<F, 8, 9>(a1, a2, xoff, xs, blocks, t, smem, s);
+    case 9 * 16 + 8: return launch_cluster_k<F, 9, 8>(a1, a2, xoff, xs, blocks, t, smem, s);
+    default: return cudaErrorNotSupported;
+    }
+}
+
+template <class F>
+cudaError_t preload_clusters_t() {
+    const cudaError_t list[] = {
+        tile_attr<F, cluster_kernel<F, 7, 7, true>>(), tile_attr<F, cluster_kernel<F, 7, 8, true>>(),
+        tile_attr<F, cluster_kernel<F, 8, 7, true>>(), tile_attr<F, cluster_kernel<F, 7, 9, true>>(),
+        tile_attr<F, cluster_kernel<F, 8, 8, true>>(), tile_attr<F, cluster_kernel<F, 9, 7, true>>(),
+        tile_attr<F, cluster_kernel<F, 8, 9, true>>(), tile_attr<F, cluster_kernel<F, 9, 8, true>>(),
+    };
+    for (cudaError_t e : list)
+        if (e != cudaSuccess)
+            return e;
+    return cudaSuccess;
 }
 
 // ---- persistent batched launch (batch.cuh)

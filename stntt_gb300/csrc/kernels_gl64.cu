@@ -129,6 +129,8 @@ cudaError_t preload_gl64() {
     cudaFuncAttributes at;
     cudaError_t e = preload_tiles_t<FieldGL>();
     if (e == cudaSuccess)
+        e = preload_clusters_t<FieldGL>();
+    if (e == cudaSuccess)
         e = cudaFuncGetAttributes(&at, gen_powers_kernel<FieldGL>);
     if (e == cudaSuccess)
         e = cudaFuncGetAttributes(&at, gen_four_step_kernel<FieldGL>);
@@ -144,6 +146,12 @@ cudaError_t preload_gl64() {
 cudaError_t gen_four_step_gl64(void *out, const void *lo, const void *hi, uint32_t h, uint32_t logS, uint64_t count,
                            uint32_t p, cudaStream_t s) {
     return gen_four_step_t<FieldGL>(out, lo, hi, h, logS, count, p, s);
+}
+
+cudaError_t launch_cluster_gl64(const PassDesc &d1, const PassDesc &d2, uint32_t p, const void *tables,
+                                const void *in, void *out, uint64_t batch, uint32_t xoff, uint32_t xs, size_t smem,
+                                cudaStream_t s) {
+    return launch_cluster_t<FieldGL>(d1, d2, p, tables, in, out, batch, xoff, xs, smem, s);
 }
 
 }  // namespace stntt

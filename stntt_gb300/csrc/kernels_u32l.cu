@@ -15,6 +15,15 @@ cudaError_t batch_launch_u32l(const void *args, const void *items, unsigned long
     return batch_launch_t<FieldU32L>(args, items, nitems, counters, ctl, smem, grid, spin_limit, s);
 }
 
-cudaError_t preload_u32l() { return preload_tiles_t<FieldU32L>(); }
+cudaError_t preload_u32l() {
+    const cudaError_t e = preload_tiles_t<FieldU32L>();
+    return e == cudaSuccess ? preload_clusters_t<FieldU32L>() : e;
+}
+
+cudaError_t launch_cluster_u32l(const PassDesc &d1, const PassDesc &d2, uint32_t p, const void *tables,
+                                const void *in, void *out, uint64_t batch, uint32_t xoff, uint32_t xs, size_t smem,
+                                cudaStream_t s) {
+    return launch_cluster_t<FieldU32L>(d1, d2, p, tables, in, out, batch, xoff, xs, smem, s);
+}
 
 }  // namespace stntt

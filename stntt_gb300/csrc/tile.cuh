@@ -112,22 +112,30 @@ struct Geo {
     bool valid;  // false for the padding rows of a partial last CTA
 };
 
-// Output k = pos of a tile's last step: the four-step twiddle w_M^(col * pos)
-// (COL; one entry of the full table with FULL4, else the product of two
-// table entries) or n^-1 (ROW with do_scale), then the canonical value to HBM.
-template <class F, bool FULL4 = false>
-__device__ __forceinline__ void store_last(const TileArgs<F> &a, const F &f, const Geo<typename F::T> &g,
-                                           uint32_t pos, typename F::T v) {
-    if (FULL4 && a.mode == kModeCol) {
-        v = f.mul_tw(v, __ldg(&a.tw4_full[(uint64_t)pos * g.ostride + g.col]));
-    } else if (a.mode == kModeCol) {
+// The four-step twiddle w_M^(col * pos) of a column pass's output pos: one
+// entry of the full table (FULL4) or the product of two table entries.
+template <class F, bool FULL4>
+__device__ __forceinline__ typename F::T four_step(const TileArgs<F> &a, const F &f, const Geo<typename F::T> &g,
+                                                   uint32_t pos, typename F::T v) {
+    if constexpr (FULL4) {
+        return f.mul_tw(v, __ldg(&a.tw4_full[(uint64_t)pos * g.ostride + g.col]));
+    } else {
         const uint64_t e = (uint64_t)g.col * pos;
         const uint32_t lo = (uint32_t)(e & ((1ull << a.h) - 1));
         const uint32_t hi = (uint32_t)(e >> a.h);
-        v = f.mul_tw(f.mul_tw(v, __ldg(&a.tw4_lo[lo])), __ldg(&a.tw4_hi[hi]));
-    } else if (a.do_scale) {
-        v = f.mul_tw(v, a.scale);
+        return f.mul_tw(f.mul_tw(v, __ldg(&a.tw4_lo[lo])), __ldg(&a.tw4_hi[hi]));
     }
+}
+
+// Output k = pos of a tile's last step: the four-step twiddle (COL) or n^-1
+// (ROW with do_scale), then the canonical value to HBM.
+template <class F, bool FULL4 = false>
+__device__ __forceinline__ void store_last(const TileArgs<F> &a, const F &f, const Geo<typename F::T> &g,
+                                           uint32_t pos, typename F::T v) {
+    if (a.mode == kModeCol)
+        v = four_step<F, FULL4>(a, f, g, pos, v);
+    else if (a.do_scale)
+        v = f.mul_tw(v, a.scale);
     v = f.canon(v);
     if (g.valid)
         g.dst[(uint64_t)pos * g.ostride] = v;
@@ -308,6 +316,18 @@ __global__ void __launch_bounds__(E >= 32 ? 512 : 1024) tile_kernel(const TileAr
     tile_run<F, E, TAIL, IN2>(a, blockIdx.x, reinterpret_cast<typename F::T *>(smem_raw));
 }
 
+// Where a tile's first step reads and its last step writes: HBM through the
+// tile geometry (the four-step twiddle or scale applied on the way out).
+template <class F, bool FULL4>
+struct GlobalIO {
+    using T = typename F::T;
+    Geo<T> g;
+    __device__ __forceinline__ T load(uint32_t idx) const { return g.valid ? g.src[(uint64_t)idx * g.istride] : T(0); }
+    __device__ __forceinline__ void store(const TileArgs<F> &a, const F &f, uint32_t pos, T v) const {
+        store_last<F, FULL4>(a, f, g, pos, v);
+    }
+};
+
 // ---- Tile length fixed at compile time -----------------------------------
 // The same Stockham steps with L = 2^LOGL a template parameter and 16
 // elements per thread: each step's stride, twiddle shift and output spacing
@@ -315,9 +335,9 @@ __global__ void __launch_bounds__(E >= 32 ? 512 : 1024) tile_kernel(const TileAr
 // an immediate. The padding never separates an access from its base:
 // Pad(b + d) = Pad(b) + d + (d >> PS) for every read (b = u, d = m U + r L/R)
 // and every write (b = the item's output base, d = r p) of these steps.
-template <class F, int E, int LOGL, int LOGR, int LOGP, bool first, bool last, bool FULL4>
+template <class F, int E, int LOGL, int LOGR, int LOGP, bool first, bool last, class IO>
 __device__ __forceinline__ void tile_step_l(const TileArgs<F> &a, const F &f, typename F::T (&x)[E],
-                                            typename F::T *col_sm, uint32_t u, const Geo<typename F::T> &g) {
+                                            typename F::T *col_sm, uint32_t u, const IO &io) {
     using T = typename F::T;
     constexpr int R = 1 << LOGR, ITEMS = E / R;
     constexpr uint32_t PS = Pad<F>::PS, U = (1u << LOGL) / E, TS = (1u << LOGL) >> LOGR, P = 1u << LOGP;
@@ -330,7 +350,7 @@ __device__ __forceinline__ void tile_step_l(const TileArgs<F> &a, const F &f, ty
         for (int r = 0; r < R; ++r) {
             const uint32_t d = m * U + r * TS;
             if constexpr (first)
-                x[m * R + r] = g.valid ? g.src[(uint64_t)(u + d) * g.istride] : T(0);
+                x[m * R + r] = io.load(u + d);
             else
                 x[m * R + r] = col_sm[pu + d + (d >> PS)];
         }
@@ -360,7 +380,7 @@ __device__ __forceinline__ void tile_step_l(const TileArgs<F> &a, const F &f, ty
             const uint32_t d = (uint32_t)r << LOGP;
             const T v = x[m * R + bit_reverse<LOGR>(r)];
             if constexpr (last)
-                store_last<F, FULL4>(a, f, g, base + d, v);
+                io.store(a, f, base + d, v);
             else
                 col_sm[pb + d + (d >> PS)] = v;
         }
@@ -371,16 +391,16 @@ __device__ __forceinline__ void tile_step_l(const TileArgs<F> &a, const F &f, ty
 
 // Steps S.. of a 2^LOGL tile: one leading radix-2^(LOGL mod 4) step when LOGL
 // is not a multiple of 4, then radix-16 steps.
-template <class F, int E, int LOGL, int S, bool FULL4>
+template <class F, int E, int LOGL, int S, class IO>
 __device__ __forceinline__ void tile_steps_l(const TileArgs<F> &a, const F &f, typename F::T (&x)[E],
-                                             typename F::T *col_sm, uint32_t u, const Geo<typename F::T> &g) {
+                                             typename F::T *col_sm, uint32_t u, const IO &io) {
     constexpr int TAIL = LOGL & 3;
     constexpr int NS = (LOGL >> 2) + (TAIL > 0 ? 1 : 0);
     if constexpr (S < NS) {
         constexpr int LOGR = (S == 0 && TAIL > 0) ? TAIL : 4;
         constexpr int LOGP = S == 0 ? 0 : (TAIL > 0 ? TAIL + 4 * (S - 1) : 4 * S);
-        tile_step_l<F, E, LOGL, LOGR, LOGP, S == 0, S == NS - 1, FULL4>(a, f, x, col_sm, u, g);
-        tile_steps_l<F, E, LOGL, S + 1, FULL4>(a, f, x, col_sm, u, g);
+        tile_step_l<F, E, LOGL, LOGR, LOGP, S == 0, S == NS - 1, IO>(a, f, x, col_sm, u, io);
+        tile_steps_l<F, E, LOGL, S + 1, IO>(a, f, x, col_sm, u, io);
     }
 }
 
@@ -395,7 +415,7 @@ __device__ __forceinline__ void tile_run_l(const TileArgs<F> &a, uint64_t blk, t
     uint32_t c, u;
     const Geo<T> g = tile_geo<F, 16>(a, blk, c, u);
     T x[16];
-    tile_steps_l<F, 16, LOGL, 0, FULL4>(a, f, x, sm + c * a.cs, u, g);
+    tile_steps_l<F, 16, LOGL, 0, GlobalIO<F, FULL4>>(a, f, x, sm + c * a.cs, u, GlobalIO<F, FULL4>{g});
 }
 
 template <class F, int LOGL, bool FULL4 = false>
