@@ -533,11 +533,15 @@ int check_u32_args(stntt_ctx *ctx, uint32_t log_n, uint32_t p, uint32_t root) {
 // A two-pass plan's passes as one launch of 8-CTA clusters: CTA r takes n2/8
 // columns in the first pass and n1/8 rows in the second, exchanging through
 // distributed shared memory. STNTT_EUNSUPPORTED when the shape does not fit
-// (tile lengths 2^7..2^9 with 16 elements per thread, the shared memory of a
-// CTA, a prime without the lazy kernels).
+// (tile lengths 2^7..2^9 with 16 elements per thread, at most 256 KiB per
+// transform, the shared memory of a CTA, a prime without the lazy kernels).
 int run_cluster(stntt_ctx *ctx, const Plan &pl, const void *in, void *out, uint64_t batch, cudaStream_t s) {
     const PassDesc &p1 = pl.passes[0], &p2 = pl.passes[1];
     if (p1.E != 16 || p2.E != 16 || p1.mode != kModeCol || p2.mode != kModeRow)
+        return STNTT_EUNSUPPORTED;
+    // Up to 256 KiB per transform: beyond that 8 SMs are compute-bound and the
+    // two-pass launches were as fast or faster (measured, 2^16 Goldilocks, 2^17 32-bit).
+    if ((pl.field == kFieldGL ? 8ull : 4ull) << pl.log_n > (256ull << 10))
         return STNTT_EUNSUPPORTED;
     const uint32_t L1 = p1.logL, L2 = p2.logL;
     if (L1 < 7 || L1 > 9 || L2 < 7 || L2 > 9 || L1 + L2 < 14 || L1 + L2 > 17)
