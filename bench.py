@@ -460,7 +460,7 @@ def main():
         fwd = lambda: ctx.ntt_u32(data, lg, 1, p, root, inverse=False, stream=sp)  # noqa: E731
         inv = lambda: ctx.ntt_u32(data, lg, 1, p, root, inverse=True, stream=sp)  # noqa: E731
         fid = st.FIELD_U32
-    passes, pass_logs = ctx.plan_info(fid, lg, p, root)
+    passes, pass_logs = ctx.call_info(fid, lg, 1, p, root)  # kernel launches one call of this shape makes
     stream.synchronize()
     ref_copy = data.clone()
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.int32, device=dev)

@@ -87,6 +87,13 @@ int stntt_prepare(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t p, uint32_
 int stntt_plan_info(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t p, uint32_t root, int dir,
                     uint32_t *passes, uint32_t *pass_logs);
 
+/* What one call of this shape does: the number of kernel launches per
+ * transform call (1 when both passes of a small two-pass plan run as one
+ * thread-block-cluster launch) and log2 of each pass's tile length (up to 4),
+ * for the plan a call with this batch uses. */
+int stntt_call_info(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t batch, uint32_t p, uint32_t root, int dir,
+                    uint32_t *launches, uint32_t *pass_logs);
+
 /* Override the plan for one (field, log_n): npasses HBM passes (1..4) with
  * tile lengths 2^pass_logs[i] (summing to log_n, each <= 13; npasses <= 3), elements per
  * thread elems[i] (16 or 32; 0 = default) and columns per CTA cols[i] (a power

@@ -96,6 +96,7 @@ _SIGS = {
     "stntt_plan_info": (_int, [_vp, _int, _u32, _u32, _u32, _int, C.POINTER(_u32), C.POINTER(_u32)]),
     "stntt_set_plan": (_int, [_vp, _int, _u32, _u32, C.POINTER(_u32), C.POINTER(_u32), C.POINTER(_u32)]),
     "stntt_set_plan_small": (_int, [_vp, _int, _u32, _u32, C.POINTER(_u32), C.POINTER(_u32), C.POINTER(_u32)]),
+    "stntt_call_info": (_int, [_vp, _int, _u32, _u32, _u32, _u32, _int, C.POINTER(_u32), C.POINTER(_u32)]),
     "stntt_clear_plans": (_int, [_vp]),
     "stntt_device_key": (_int, [_int, C.c_char_p, _sz]),
     "stntt_ntt_u32": (_int, [_vp, _vp, _u32, _u32, _u32, _u32, _int, _u32, _vp]),
@@ -281,6 +282,14 @@ class Context:
         _check(lib().stntt_plan_info(self._h, field, log_n, p, root, INVERSE if inverse else FORWARD,
                                      C.byref(n), logs), self._h)
         return n.value, list(logs)[: n.value]
+
+    def call_info(self, field: int, log_n: int, batch: int = 1, p: int = 0, root: int = 0, inverse: bool = False):
+        """(kernel launches per call, [log2 tile length per pass]) for a call of this shape."""
+        n = _u32()
+        logs = (_u32 * 4)()
+        _check(lib().stntt_call_info(self._h, field, log_n, batch, p, root, INVERSE if inverse else FORWARD,
+                                     C.byref(n), logs), self._h)
+        return n.value, [v for v in logs if v]
 
     def set_plan(self, field: int, log_n: int, pass_logs, elems=None, cols=None, small: bool = False) -> None:
         """Override the plan shape for one size (stntt_set_plan); small=True sets

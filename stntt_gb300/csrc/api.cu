@@ -535,30 +535,45 @@ int check_u32_args(stntt_ctx *ctx, uint32_t log_n, uint32_t p, uint32_t root) {
 // distributed shared memory. STNTT_EUNSUPPORTED when the shape does not fit
 // (tile lengths 2^7..2^9 with 16 elements per thread, at most 256 KiB per
 // transform, the shared memory of a CTA, a prime without the lazy kernels).
-int run_cluster(stntt_ctx *ctx, const Plan &pl, const void *in, void *out, uint64_t batch, cudaStream_t s) {
+struct ClusterShape {
+    PassDesc d1, d2;
+    uint32_t xoff = 0, xs = 0;
+    size_t smem = 0;
+};
+
+bool cluster_shape(const Plan &pl, ClusterShape &cs) {
+    if (pl.passes.size() != 2 || (pl.field != kFieldGL && pl.p >= (1u << 30)))
+        return false;
     const PassDesc &p1 = pl.passes[0], &p2 = pl.passes[1];
-    if (p1.E != 16 || p2.E != 16 || p1.mode != kModeCol || p2.mode != kModeRow)
-        return STNTT_EUNSUPPORTED;
+    if (p1.E != 16 || p2.E != 16 || p1.mode != kModeCol || p2.mode != kModeRow || p1.full_off == ~0ull)
+        return false;
     // Up to 256 KiB per transform: beyond that 8 SMs are compute-bound and the
     // two-pass launches were as fast or faster (measured, 2^16 Goldilocks, 2^17 32-bit).
     if ((pl.field == kFieldGL ? 8ull : 4ull) << pl.log_n > (256ull << 10))
-        return STNTT_EUNSUPPORTED;
+        return false;
     const uint32_t L1 = p1.logL, L2 = p2.logL;
     if (L1 < 7 || L1 > 9 || L2 < 7 || L2 > 9 || L1 + L2 < 14 || L1 + L2 > 17)
-        return STNTT_EUNSUPPORTED;
-    PassDesc d1 = p1, d2 = p2;
-    shape_pass(d1, pl.field, 1ull << p1.logS, 16, 1u << (L2 - kClusterLog));  // column limit: the sub-problem's columns
-    shape_pass(d2, pl.field, 1ull << 20, 16, 1u << (L1 - kClusterLog));
-    if (d1.logC != L2 - kClusterLog || d2.logC != L1 - kClusterLog || d1.threads != d2.threads)
-        return STNTT_EUNSUPPORTED;
+        return false;
+    cs.d1 = p1;
+    cs.d2 = p2;
+    shape_pass(cs.d1, pl.field, 1ull << p1.logS, 16, 1u << (L2 - kClusterLog));  // column limit: the sub-problem's columns
+    shape_pass(cs.d2, pl.field, 1ull << 20, 16, 1u << (L1 - kClusterLog));
+    if (cs.d1.logC != L2 - kClusterLog || cs.d2.logC != L1 - kClusterLog || cs.d1.threads != cs.d2.threads)
+        return false;
     const size_t esz = pl.field == kFieldGL ? 8 : 4;
-    const uint32_t xs = (1u << L1) + 1;  // odd: conflict-free column writes and row gathers
-    const uint64_t work = std::max<uint64_t>((uint64_t)d1.cs << d1.logC, (uint64_t)d2.cs << d2.logC);
-    const uint32_t xoff = (uint32_t)((work + 3) & ~3ull);
-    const size_t smem = (xoff + ((uint64_t)xs << d1.logC)) * esz;
-    if (smem > 200 * 1024)
+    cs.xs = (1u << L1) + 1;  // odd: conflict-free column writes and row gathers
+    const uint64_t work = std::max<uint64_t>((uint64_t)cs.d1.cs << cs.d1.logC, (uint64_t)cs.d2.cs << cs.d2.logC);
+    cs.xoff = (uint32_t)((work + 3) & ~3ull);
+    cs.smem = (cs.xoff + ((uint64_t)cs.xs << cs.d1.logC)) * esz;
+    return cs.smem <= 200 * 1024;
+}
+
+int run_cluster(stntt_ctx *ctx, const Plan &pl, const void *in, void *out, uint64_t batch, cudaStream_t s) {
+    ClusterShape cs;
+    if (!cluster_shape(pl, cs))
         return STNTT_EUNSUPPORTED;
-    const cudaError_t e = launch_cluster(pl.field, d1, d2, pl.p, pl.d_tables, in, out, batch, xoff, xs, smem, s);
+    const cudaError_t e =
+        launch_cluster(pl.field, cs.d1, cs.d2, pl.p, pl.d_tables, in, out, batch, cs.xoff, cs.xs, cs.smem, s);
     if (e == cudaErrorNotSupported)
         return STNTT_EUNSUPPORTED;
     return e == cudaSuccess ? STNTT_OK : cuda_fail(ctx, e, "cluster launch");
@@ -951,6 +966,42 @@ int set_plan_for(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t npasses, co
 }
 
 }  // namespace
+
+int stntt_call_info(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t batch, uint32_t p, uint32_t root, int dir,
+                    uint32_t *launches, uint32_t *pass_logs) {
+    if (!ctx || !launches || batch == 0)
+        return STNTT_EINVAL;
+    if (dir != STNTT_FORWARD && dir != STNTT_INVERSE)
+        return fail(ctx, STNTT_EINVAL, "call_info: bad direction");
+    int f;
+    uint64_t r = root;
+    if (field == STNTT_FIELD_GL64) {
+        if (log_n > 32)
+            return fail(ctx, STNTT_EUNSUPPORTED, "log_n must be <= 32 for Goldilocks");
+        f = kFieldGL;
+        p = 0;
+        stntt_gl64_root(log_n, &r);
+    } else if (field == STNTT_FIELD_U32) {
+        const int rc = check_u32_args(ctx, log_n, p, root);
+        if (rc)
+            return rc;
+        f = kFieldU32;
+    } else {
+        return fail(ctx, STNTT_EINVAL, "call_info: unknown field");
+    }
+    DeviceGuard g(ctx->device);
+    const Plan *pl;
+    const int rc = get_plan(ctx, f, log_n, p, r, dir, &pl, ((uint64_t)batch << log_n) < kSmallCallElems);
+    if (rc)
+        return rc;
+    ClusterShape cs;
+    const bool cluster = ((uint64_t)batch << log_n) < kSmallCallElems && cluster_shape(*pl, cs);
+    *launches = cluster ? 1u : (uint32_t)pl->passes.size();
+    if (pass_logs)
+        for (size_t i = 0; i < pl->passes.size() && i < 4; ++i)
+            pass_logs[i] = pl->passes[i].logL;
+    return STNTT_OK;
+}
 
 int stntt_set_plan(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t npasses, const uint32_t *pass_logs,
                    const uint32_t *elems, const uint32_t *cols) {

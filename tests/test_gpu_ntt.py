@@ -485,3 +485,48 @@ def test_small_call_plans(ctx):
         ctx.clear_plans()
         from stntt_gb300 import tune
         tune.apply_cache(ctx)
+
+
+@pytest.mark.parametrize("field,lg", [("u32", 14), ("u32", 15), ("u32", 16), ("gl64", 14), ("gl64", 15)])
+def test_cluster_path(ctx, field, lg):
+    """Small two-pass calls run as one thread-block-cluster launch (both passes
+    exchanging through distributed shared memory): batches of 1, 3 and 8,
+    forward and inverse, in place and out of place, equal the oracle."""
+    n = 1 << lg
+    for batch in (1, 3, 8):
+        if field == "gl64":
+            x = O.uniform_u64(500 + lg + batch, batch * n)
+            want = O.ntt_gl64(x, batch=batch, threads=8)
+            d = dev64(x)
+            o = torch.empty_like(d)
+            ctx.ntt_gl64_oop(d, o, lg, batch)
+            assert np.array_equal(host64(o), want), (lg, batch)
+            ctx.ntt_gl64(d, lg, batch)
+            assert np.array_equal(host64(d), want), (lg, batch)
+            ctx.ntt_gl64(d, lg, batch, inverse=True)
+            assert np.array_equal(host64(d), x), (lg, batch)
+        else:
+            p, root = st.params_u32(lg)
+            x = O.uniform_u32(500 + lg + batch, p, batch * n)
+            want = O.ntt_u32(x, root, p, batch=batch, threads=8)
+            d = dev32(x)
+            o = torch.empty_like(d)
+            ctx.ntt_u32_oop(d, o, lg, batch, p, root)
+            assert np.array_equal(host32(o), want), (lg, batch)
+            ctx.ntt_u32(d, lg, batch, p, root)
+            assert np.array_equal(host32(d), want), (lg, batch)
+            ctx.ntt_u32(d, lg, batch, p, root, inverse=True)
+            assert np.array_equal(host32(d), x), (lg, batch)
+
+
+def test_call_info_reports_launches(ctx):
+    """stntt_call_info: one launch for a small call on the cluster path, the
+    plan's pass count otherwise."""
+    p16, r16 = st.params_u32(16)
+    assert ctx.call_info(st.FIELD_U32, 16, 1, p16, r16)[0] == 1
+    n, logs = ctx.call_info(st.FIELD_U32, 16, 64, p16, r16)  # 2^22 elements: not a small call
+    assert n == len(logs) >= 2 and sum(logs) == 16
+    n, logs = ctx.call_info(st.FIELD_GL64, 16, 1)  # 512 KiB: the two-pass launches
+    assert n == len(logs) == 2 and sum(logs) == 16
+    n, logs = ctx.call_info(st.FIELD_GL64, 24, 1)
+    assert n == len(logs) and sum(logs) == 24
