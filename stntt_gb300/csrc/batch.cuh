@@ -40,6 +40,12 @@ constexpr int kBatchThreads = 512;  // C * L / 16 for every item
 // bodies and the persistent loop around them.
 template <class F, int LOGL>
 __device__ __noinline__ void batch_item_l(const TileArgs<F> &a, uint64_t blk, typename F::T *sm) {
+    if constexpr (LOGL >= 6) {
+        if (a.tw4_full && a.mode == kModeCol) {  // column pass with a full four-step table
+            tile_run_l<F, LOGL, true>(a, blk, sm);
+            return;
+        }
+    }
     tile_run_l<F, LOGL>(a, blk, sm);
 }
 
