@@ -50,9 +50,9 @@ cudaError_t copy_scale_gl64(const void *, void *, size_t, uint64_t, cudaStream_t
 cudaError_t launch_gl_probe(uint64_t *, unsigned, int, cudaStream_t);
 cudaError_t preload_u32();
 cudaError_t launch_cluster_u32l(const PassDesc &, const PassDesc &, uint32_t, const void *, const void *, void *,
-                                uint64_t, uint32_t, uint32_t, size_t, cudaStream_t);
+                                uint64_t, uint32_t, uint32_t, size_t, uint32_t, cudaStream_t);
 cudaError_t launch_cluster_gl64(const PassDesc &, const PassDesc &, uint32_t, const void *, const void *, void *,
-                                uint64_t, uint32_t, uint32_t, size_t, cudaStream_t);
+                                uint64_t, uint32_t, uint32_t, size_t, uint32_t, cudaStream_t);
 cudaError_t preload_u32l();
 cudaError_t preload_gl64();
 size_t batch_args_size_u32();
@@ -115,11 +115,11 @@ cudaError_t launch_gen_powers(int field, void *out, uint64_t count, uint64_t bas
 }
 cudaError_t launch_cluster(int field, const PassDesc &d1, const PassDesc &d2, uint32_t p, const void *tables,
                            const void *in, void *out, uint64_t batch, uint32_t xoff, uint32_t xs, size_t smem,
-                           cudaStream_t s) {
+                           uint32_t log_k, cudaStream_t s) {
     if (field == kFieldGL)
-        return launch_cluster_gl64(d1, d2, p, tables, in, out, batch, xoff, xs, smem, s);
+        return launch_cluster_gl64(d1, d2, p, tables, in, out, batch, xoff, xs, smem, log_k, s);
     if (p < (1u << 30))
-        return launch_cluster_u32l(d1, d2, p, tables, in, out, batch, xoff, xs, smem, s);
+        return launch_cluster_u32l(d1, d2, p, tables, in, out, batch, xoff, xs, smem, log_k, s);
     return cudaErrorNotSupported;
 }
 cudaError_t launch_gen_four_step(int field, void *out, const void *lo, const void *hi, uint32_t h, uint32_t logS,
@@ -231,6 +231,7 @@ struct stntt_ctx {
     DevBuf host_stage;
     std::string err;
     size_t mem = 0;
+    uint32_t cluster_log = 3;  // log2 of the cluster size the one-launch transforms use (3 or 4)
 };
 
 namespace sd {
@@ -530,35 +531,38 @@ int check_u32_args(stntt_ctx *ctx, uint32_t log_n, uint32_t p, uint32_t root) {
     return STNTT_OK;
 }
 
-// A two-pass plan's passes as one launch of 8-CTA clusters: CTA r takes n2/8
-// columns in the first pass and n1/8 rows in the second, exchanging through
+// A two-pass plan's passes as one launch of K-CTA clusters: CTA r takes n2/K
+// columns in the first pass and n1/K rows in the second, exchanging through
 // distributed shared memory. STNTT_EUNSUPPORTED when the shape does not fit
-// (tile lengths 2^7..2^9 with 16 elements per thread, at most 256 KiB per
-// transform, the shared memory of a CTA, a prime without the lazy kernels).
+// (tile lengths 2^7..2^9 with 16 elements per thread, at most 32 KiB of the
+// transform per CTA, the shared memory of a CTA, a prime without the lazy
+// kernels).
 struct ClusterShape {
     PassDesc d1, d2;
-    uint32_t xoff = 0, xs = 0;
+    uint32_t xoff = 0, xs = 0, log_k = 3;
     size_t smem = 0;
 };
 
-bool cluster_shape(const Plan &pl, ClusterShape &cs) {
+bool cluster_shape(const Plan &pl, uint32_t log_k, ClusterShape &cs) {
     if (pl.passes.size() != 2 || (pl.field != kFieldGL && pl.p >= (1u << 30)))
         return false;
     const PassDesc &p1 = pl.passes[0], &p2 = pl.passes[1];
     if (p1.E != 16 || p2.E != 16 || p1.mode != kModeCol || p2.mode != kModeRow || p1.full_off == ~0ull)
         return false;
-    // Up to 256 KiB per transform: beyond that 8 SMs are compute-bound and the
-    // two-pass launches were as fast or faster (measured, 2^16 Goldilocks, 2^17 32-bit).
-    if ((pl.field == kFieldGL ? 8ull : 4ull) << pl.log_n > (256ull << 10))
+    // Up to 32 KiB per CTA of the cluster (256 KiB for 8 CTAs, 512 KiB for 16):
+    // beyond that the cluster's SMs are compute-bound and the two-pass launches
+    // were as fast or faster (measured: 8 CTAs at 2^16 Goldilocks, 2^17 32-bit).
+    if ((pl.field == kFieldGL ? 8ull : 4ull) << pl.log_n > (32ull << (10 + log_k)))
         return false;
     const uint32_t L1 = p1.logL, L2 = p2.logL;
     if (L1 < 7 || L1 > 9 || L2 < 7 || L2 > 9 || L1 + L2 < 14 || L1 + L2 > 17)
         return false;
     cs.d1 = p1;
     cs.d2 = p2;
-    shape_pass(cs.d1, pl.field, 1ull << p1.logS, 16, 1u << (L2 - kClusterLog));  // column limit: the sub-problem's columns
-    shape_pass(cs.d2, pl.field, 1ull << 20, 16, 1u << (L1 - kClusterLog));
-    if (cs.d1.logC != L2 - kClusterLog || cs.d2.logC != L1 - kClusterLog || cs.d1.threads != cs.d2.threads)
+    cs.log_k = log_k;
+    shape_pass(cs.d1, pl.field, 1ull << p1.logS, 16, 1u << (L2 - log_k));  // column limit: the sub-problem's columns
+    shape_pass(cs.d2, pl.field, 1ull << 20, 16, 1u << (L1 - log_k));
+    if (cs.d1.logC != L2 - log_k || cs.d2.logC != L1 - log_k || cs.d1.threads != cs.d2.threads)
         return false;
     const size_t esz = pl.field == kFieldGL ? 8 : 4;
     cs.xs = (1u << L1) + 1;  // odd: conflict-free column writes and row gathers
@@ -568,12 +572,19 @@ bool cluster_shape(const Plan &pl, ClusterShape &cs) {
     return cs.smem <= 200 * 1024;
 }
 
+// The cluster shape for this context: 16 CTAs where the device schedules them,
+// else (or when 16 does not fit the plan) 8.
+bool cluster_shape(const stntt_ctx *ctx, const Plan &pl, ClusterShape &cs) {
+    return (ctx->cluster_log > kClusterLogSmall && cluster_shape(pl, ctx->cluster_log, cs)) ||
+           cluster_shape(pl, kClusterLogSmall, cs);
+}
+
 int run_cluster(stntt_ctx *ctx, const Plan &pl, const void *in, void *out, uint64_t batch, cudaStream_t s) {
     ClusterShape cs;
-    if (!cluster_shape(pl, cs))
+    if (!cluster_shape(ctx, pl, cs))
         return STNTT_EUNSUPPORTED;
-    const cudaError_t e =
-        launch_cluster(pl.field, cs.d1, cs.d2, pl.p, pl.d_tables, in, out, batch, cs.xoff, cs.xs, cs.smem, s);
+    const cudaError_t e = launch_cluster(pl.field, cs.d1, cs.d2, pl.p, pl.d_tables, in, out, batch, cs.xoff, cs.xs,
+                                         cs.smem, cs.log_k, s);
     if (e == cudaErrorNotSupported)
         return STNTT_EUNSUPPORTED;
     return e == cudaSuccess ? STNTT_OK : cuda_fail(ctx, e, "cluster launch");
@@ -778,6 +789,8 @@ int stntt_init(stntt_ctx **out, int device) {
         delete ctx;
         return STNTT_ECUDA;
     }
+    if (cluster_max_size() >= 16)
+        ctx->cluster_log = kClusterLogLarge;
     // Load every kernel now: a lazy load at first use would stall the device
     // in the middle of a caller's stream of work. This also fails early when
     // the library holds no code for this GPU.
@@ -995,7 +1008,7 @@ int stntt_call_info(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t batch, u
     if (rc)
         return rc;
     ClusterShape cs;
-    const bool cluster = ((uint64_t)batch << log_n) < kSmallCallElems && cluster_shape(*pl, cs);
+    const bool cluster = ((uint64_t)batch << log_n) < kSmallCallElems && cluster_shape(ctx, *pl, cs);
     *launches = cluster ? 1u : (uint32_t)pl->passes.size();
     if (pass_logs)
         for (size_t i = 0; i < pl->passes.size() && i < 4; ++i)

@@ -1,16 +1,17 @@
-// cluster.cuh -- a whole two-pass transform in one launch: a cluster of 8
-// CTAs holds it in distributed shared memory.
+// cluster.cuh -- a whole two-pass transform in one launch: a cluster of K
+// CTAs (16 where the device schedules them, else 8) holds it in distributed
+// shared memory.
 //
 // For n = n1 * n2 (n1 = 2^LOG1 column length, n2 = 2^LOG2 row length), the
 // same two passes as a two-pass plan (same twiddle tables and arithmetic) run
 // back to back inside one cluster per transform:
-//   phase 1: CTA r of the cluster takes columns [r n2/8, (r+1) n2/8), reads
+//   phase 1: CTA r of the cluster takes columns [r n2/K, (r+1) n2/K), reads
 //     them from HBM, transforms them and writes each result, after the
 //     four-step twiddle, into its own exchange buffer (column-major, odd
 //     stride, so that neither these writes nor the phase-2 reads conflict);
 //   cluster barrier (every exchange buffer complete);
-//   phase 2: CTA r takes rows [r n1/8, (r+1) n1/8); element j of row k1 is
-//     element k1 of column j, read from the exchange buffer of CTA j / (n2/8)
+//   phase 2: CTA r takes rows [r n1/K, (r+1) n1/K); element j of row k1 is
+//     element k1 of column j, read from the exchange buffer of CTA j / (n2/K)
 //     through distributed shared memory; the row transform's output goes to
 //     HBM in the digit-reversed order of the row pass;
 //   cluster barrier (no CTA leaves while another still reads its buffer).
@@ -52,9 +53,9 @@ struct ClusterGatherIO {
     }
 };
 
-// a1 / a2: the plan's two passes, reshaped to n2/8 columns and n1/8 rows per
+// a1 / a2: the plan's two passes, reshaped to n2/K columns and n1/K rows per
 // CTA. xoff: element offset of the exchange buffer in shared memory; xs: its
-// column stride. Grid: 8 CTAs per transform, cluster dimension 8.
+// column stride. Grid: K CTAs per transform, cluster dimension K.
 template <class F, int LOG1, int LOG2, bool FULL4>
 __global__ void __launch_bounds__(1024) cluster_kernel(const TileArgs<F> a1, const TileArgs<F> a2, uint32_t xoff,
                                                        uint32_t xs) {
@@ -63,7 +64,7 @@ __global__ void __launch_bounds__(1024) cluster_kernel(const TileArgs<F> a1, con
     T *work = reinterpret_cast<T *>(smem_raw);
     T *xbuf = work + xoff;
     cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
-    const uint64_t blk = blockIdx.x;  // tile index over the batch: transform (blk >> 3), cluster rank (blk & 7)
+    const uint64_t blk = blockIdx.x;  // tile index over the batch: transform blk / K, cluster rank blk mod K
     F f;
     f.p = a1.p;
     T x[16];

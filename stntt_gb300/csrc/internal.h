@@ -15,7 +15,9 @@ enum : uint32_t { kModeCol = 0, kModeRow = 1 };  // tile pass kinds (tile.cuh)
 // batch and the sub-problems); larger ones, whose table would stream from
 // HBM on the store path, keep the two-level lookup.
 constexpr uint32_t kFullTwiddleMinLog = 14, kFullTwiddleMaxLog = 20;
-constexpr uint32_t kClusterLog = 3;  // one-launch transforms: 8 CTAs per cluster (portable size)
+// One-launch transforms: 16-CTA clusters (non-portable size) where the device
+// schedules them, else 8; up to 2^(15 + log2 K) bytes per transform.
+constexpr uint32_t kClusterLogSmall = 3, kClusterLogLarge = 4;
 
 // One HBM pass of a transform plan (see tile.cuh for the meaning of the fields).
 struct PassDesc {
@@ -40,7 +42,9 @@ cudaError_t launch_gen_powers(int field, void *out, uint64_t count, uint64_t bas
 // cudaErrorNotSupported when this plan or prime cannot use it.
 cudaError_t launch_cluster(int field, const PassDesc &d1, const PassDesc &d2, uint32_t p, const void *tables,
                            const void *in, void *out, uint64_t batch, uint32_t xoff, uint32_t xs, size_t smem,
-                           cudaStream_t s);
+                           uint32_t log_k, cudaStream_t s);
+// Largest cluster the current device schedules for the cluster kernels (8 or 16).
+int cluster_max_size();
 // out[pos * 2^logS + col] = w_M^(col * pos) for count = M entries, from the
 // two-level tables lo (w_M^e, e < 2^h) and hi (s * w_M^(e 2^h)).
 cudaError_t launch_gen_four_step(int field, void *out, const void *lo, const void *hi, uint32_t h, uint32_t logS,

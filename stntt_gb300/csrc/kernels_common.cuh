@@ -86,11 +86,32 @@ bool launch_tile_fixed(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks,
 }
 
 // ---- one-launch transforms in a thread-block cluster (cluster.cuh)
+// Shared-memory limit and permission for 16-CTA clusters, once per device.
+template <class F, auto KERN>
+cudaError_t cluster_attr() {
+    static bool attr_set[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+        return e;
+    if (dev < 0 || dev >= 64)
+        return cudaErrorInvalidDevice;
+    if (!attr_set[dev]) {
+        e = cudaFuncSetAttribute(KERN, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(KERN, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        if (e != cudaSuccess)
+            return e;
+        attr_set[dev] = true;
+    }
+    return cudaSuccess;
+}
+
 template <class F, int LOG1, int LOG2>
 cudaError_t launch_cluster_k(const TileArgs<F> &a1, const TileArgs<F> &a2, uint32_t xoff, uint32_t xs,
-                             uint64_t blocks, uint32_t threads, size_t smem, cudaStream_t s) {
+                             uint64_t blocks, uint32_t threads, size_t smem, uint32_t log_k, cudaStream_t s) {
     auto kern = cluster_kernel<F, LOG1, LOG2, true>;
-    cudaError_t e = tile_attr<F, cluster_kernel<F, LOG1, LOG2, true>>();
+    cudaError_t e = cluster_attr<F, cluster_kernel<F, LOG1, LOG2, true>>();
     if (e != cudaSuccess)
         return e;
     if (smem > 200 * 1024 || blocks > 0x7fffffffull)
@@ -102,7 +123,7 @@ cudaError_t launch_cluster_k(const TileArgs<F> &a1, const TileArgs<F> &a2, uint3
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = 1u << kClusterLog;
+    attr[0].val.clusterDim.x = 1u << log_k;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
@@ -198,13 +219,14 @@ cudaError_t launch_tile_t(const PassDesc &d, uint32_t p, const void *tables, con
     }
 }
 
-// Both passes of a two-pass plan in one cluster launch: d1 / d2 already hold
-// n2/8 columns and n1/8 rows per CTA. cudaErrorNotSupported when this split
+// Both passes of a two-pass plan in one launch of clusters of 2^log_k CTAs:
+// d1 / d2 already hold n2 / K columns and n1 / K rows per CTA. cudaErrorNotSupported when this split
 // (tile lengths 2^7..2^9, n = 2^14..2^17) or a missing full four-step table
 // rules it out; the caller then launches the two passes.
 template <class F>
 cudaError_t launch_cluster_t(const PassDesc &d1, const PassDesc &d2, uint32_t p, const void *tables, const void *in,
-                             void *out, uint64_t batch, uint32_t xoff, uint32_t xs, size_t smem, cudaStream_t s) {
+                             void *out, uint64_t batch, uint32_t xoff, uint32_t xs, size_t smem, uint32_t log_k,
+                             cudaStream_t s) {
     TileArgs<F> a1, a2;
     fill_args<F>(a1, d1, p, tables, in, nullptr);
     fill_args<F>(a2, d2, p, tables, nullptr, out);
@@ -212,28 +234,54 @@ cudaError_t launch_cluster_t(const PassDesc &d1, const PassDesc &d2, uint32_t p,
     a2.total = batch << (d2.logN - d2.logL);
     if (!a1.tw4_full)
         return cudaErrorNotSupported;
-    const uint64_t blocks = batch << kClusterLog;
+    const uint64_t blocks = batch << log_k;
     const uint32_t t = d1.threads;
     switch (d1.logL * 16 + d2.logL) {
-    case 7 * 16 + 7: return launch_cluster_k<F, 7, 7>(a1, a2, xoff, xs, blocks, t, smem, s);
-    case 7 * 16 + 8: return launch_cluster_k<F, 7, 8>(a1, a2, xoff, xs, blocks, t, smem, s);
-    case 8 * 16 + 7: return launch_cluster_k<F, 8, 7>(a1, a2, xoff, xs, blocks, t, smem, s);
-    case 7 * 16 + 9: return launch_cluster_k<F, 7, 9>(a1, a2, xoff, xs, blocks, t, smem, s);
-    case 8 * 16 + 8: return launch_cluster_k<F, 8, 8>(a1, a2, xoff, xs, blocks, t, smem, s);
-    case 9 * 16 + 7: return launch_cluster_k<F, 9, 7>(a1, a2, xoff, xs, blocks, t, smem, s);
-    case 8 * 16 + 9: return launch_cluster_k<F, 8, 9>(a1, a2, xoff, xs, blocks, t, smem, s);
-    case 9 * 16 + 8: return launch_cluster_k<F, 9, 8>(a1, a2, xoff, xs, blocks, t, smem, s);
+    case 7 * 16 + 7: return launch_cluster_k<F, 7, 7>(a1, a2, xoff, xs, blocks, t, smem, log_k, s);
+    case 7 * 16 + 8: return launch_cluster_k<F, 7, 8>(a1, a2, xoff, xs, blocks, t, smem, log_k, s);
+    case 8 * 16 + 7: return launch_cluster_k<F, 8, 7>(a1, a2, xoff, xs, blocks, t, smem, log_k, s);
+    case 7 * 16 + 9: return launch_cluster_k<F, 7, 9>(a1, a2, xoff, xs, blocks, t, smem, log_k, s);
+    case 8 * 16 + 8: return launch_cluster_k<F, 8, 8>(a1, a2, xoff, xs, blocks, t, smem, log_k, s);
+    case 9 * 16 + 7: return launch_cluster_k<F, 9, 7>(a1, a2, xoff, xs, blocks, t, smem, log_k, s);
+    case 8 * 16 + 9: return launch_cluster_k<F, 8, 9>(a1, a2, xoff, xs, blocks, t, smem, log_k, s);
+    case 9 * 16 + 8: return launch_cluster_k<F, 9, 8>(a1, a2, xoff, xs, blocks, t, smem, log_k, s);
     default: return cudaErrorNotSupported;
     }
+}
+
+// Largest cluster (8 or 16) the device schedules for one 2^16-point cluster
+// launch of this field (256 threads, its shared memory at 2^4 x 2^12 points).
+template <class F>
+int cluster_max_size_t() {
+    auto kern = cluster_kernel<F, 8, 8, true>;
+    if (cluster_attr<F, cluster_kernel<F, 8, 8, true>>() != cudaSuccess)
+        return 8;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(16);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = 80 * 1024;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 16;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&clusters, kern, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        return 8;
+    }
+    return clusters > 0 ? 16 : 8;
 }
 
 template <class F>
 cudaError_t preload_clusters_t() {
     const cudaError_t list[] = {
-        tile_attr<F, cluster_kernel<F, 7, 7, true>>(), tile_attr<F, cluster_kernel<F, 7, 8, true>>(),
-        tile_attr<F, cluster_kernel<F, 8, 7, true>>(), tile_attr<F, cluster_kernel<F, 7, 9, true>>(),
-        tile_attr<F, cluster_kernel<F, 8, 8, true>>(), tile_attr<F, cluster_kernel<F, 9, 7, true>>(),
-        tile_attr<F, cluster_kernel<F, 8, 9, true>>(), tile_attr<F, cluster_kernel<F, 9, 8, true>>(),
+        cluster_attr<F, cluster_kernel<F, 7, 7, true>>(), cluster_attr<F, cluster_kernel<F, 7, 8, true>>(),
+        cluster_attr<F, cluster_kernel<F, 8, 7, true>>(), cluster_attr<F, cluster_kernel<F, 7, 9, true>>(),
+        cluster_attr<F, cluster_kernel<F, 8, 8, true>>(), cluster_attr<F, cluster_kernel<F, 9, 7, true>>(),
+        cluster_attr<F, cluster_kernel<F, 8, 9, true>>(), cluster_attr<F, cluster_kernel<F, 9, 8, true>>(),
     };
     for (cudaError_t e : list)
         if (e != cudaSuccess)

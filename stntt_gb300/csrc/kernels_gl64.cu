@@ -150,8 +150,10 @@ cudaError_t gen_four_step_gl64(void *out, const void *lo, const void *hi, uint32
 
 cudaError_t launch_cluster_gl64(const PassDesc &d1, const PassDesc &d2, uint32_t p, const void *tables,
                                 const void *in, void *out, uint64_t batch, uint32_t xoff, uint32_t xs, size_t smem,
-                                cudaStream_t s) {
-    return launch_cluster_t<FieldGL>(d1, d2, p, tables, in, out, batch, xoff, xs, smem, s);
+                                uint32_t log_k, cudaStream_t s) {
+    return launch_cluster_t<FieldGL>(d1, d2, p, tables, in, out, batch, xoff, xs, smem, log_k, s);
 }
+
+int cluster_max_size() { return cluster_max_size_t<FieldGL>(); }
 
 }  // namespace stntt

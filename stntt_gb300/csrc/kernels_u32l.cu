@@ -22,8 +22,8 @@ cudaError_t preload_u32l() {
 
 cudaError_t launch_cluster_u32l(const PassDesc &d1, const PassDesc &d2, uint32_t p, const void *tables,
                                 const void *in, void *out, uint64_t batch, uint32_t xoff, uint32_t xs, size_t smem,
-                                cudaStream_t s) {
-    return launch_cluster_t<FieldU32L>(d1, d2, p, tables, in, out, batch, xoff, xs, smem, s);
+                                uint32_t log_k, cudaStream_t s) {
+    return launch_cluster_t<FieldU32L>(d1, d2, p, tables, in, out, batch, xoff, xs, smem, log_k, s);
 }
 
 }  // namespace stntt

@@ -526,7 +526,9 @@ def test_call_info_reports_launches(ctx):
     assert ctx.call_info(st.FIELD_U32, 16, 1, p16, r16)[0] == 1
     n, logs = ctx.call_info(st.FIELD_U32, 16, 64, p16, r16)  # 2^22 elements: not a small call
     assert n == len(logs) >= 2 and sum(logs) == 16
-    n, logs = ctx.call_info(st.FIELD_GL64, 16, 1)  # 512 KiB: the two-pass launches
-    assert n == len(logs) == 2 and sum(logs) == 16
+    n, logs = ctx.call_info(st.FIELD_GL64, 16, 1)  # 512 KiB: one 16-CTA cluster launch where the device has them
+    assert n in (1, 2) and len(logs) == 2 and sum(logs) == 16
+    n, logs = ctx.call_info(st.FIELD_GL64, 17, 1)  # 1 MiB: beyond the cluster path
+    assert n == len(logs) == 2 and sum(logs) == 17
     n, logs = ctx.call_info(st.FIELD_GL64, 24, 1)
     assert n == len(logs) and sum(logs) == 24
