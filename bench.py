@@ -63,6 +63,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--mix-jobs", type=int, default=4096, help="jobs in the batched mix (4096 for the headline)")
     ap.add_argument("--streams", type=int, default=32, help="serving: request slots")
+    ap.add_argument("--tma", choices=["auto", "on", "off"], default="auto",
+                    help="TMA-staged passes: built-in choice per pass, everywhere allowed, or never")
     return ap.parse_args()
 
 
@@ -445,6 +447,7 @@ def main():
     n = 1 << lg
     esz = 8 if field == "gl64" else 4
     ctx = st.Context(local)
+    ctx.set_tma({"auto": -1, "on": 1, "off": 0}[args.tma])
     stream = torch.cuda.Stream(device=dev)
     sp = stream.cuda_stream
     if field == "gl64":
@@ -596,7 +599,7 @@ def main():
             "config": {"workload": args.workload, "field": field, "n": n, "batch": 1,
                        "step": "forward + inverse, in place", "l2": "flushed between steps (256 MiB write)",
                        "launch": "CUDA graph per transform, replayed" if graph else "direct C-ABI calls",
-                       "parallelism": f"replicas x{world}"},
+                       "tma": args.tma, "parallelism": f"replicas x{world}"},
             "e2e": e2e, "roofline": roofline, "int_roofline": int_roofline, "cpu_baseline": cpu, "clocks": clocks,
             "gpu_launches": 2 * passes * args.steps, "round_trip_ok": ok,
         }

@@ -186,6 +186,24 @@ int stntt_batch_destroy(stntt_batch *b);
  * kernel's bounded wait gave up and reported it (the context stays usable). */
 int stntt_selftest_wait_timeout(stntt_ctx *ctx, uint32_t spin_limit);
 
+/* ---- TMA-staged passes ---------------------------------------------------------- */
+/* Passes of 2^7..2^12-point tiles can run as a persistent kernel whose tiles
+ * are copied into shared memory by the Tensor Memory Accelerator (a copy of
+ * the next tile overlaps the current tile's work). No counterpart in the
+ * reference, whose kernels load each element with its own instruction
+ * (st_ntt_global_radix2.cuh:8-86). mode: -1 = built-in choice per pass
+ * (the default), 0 = never, 1 = wherever the pass allows it. Drops cached plans. */
+int stntt_set_tma(stntt_ctx *ctx, int mode);
+/* STNTT_ETIMEOUT when a staged pass on this context gave up waiting for a copy
+ * (after about a second) since the last call -- its output is then
+ * incomplete -- else STNTT_OK. Reads a device word: synchronise the streams
+ * that ran the transforms first. Clears the word. */
+int stntt_device_status(stntt_ctx *ctx);
+/* Launch the staged kernel with no copy issued, so that its first wait runs
+ * out after spin_limit polls; returns STNTT_ETIMEOUT when the kernel reported
+ * it (the context stays usable). */
+int stntt_selftest_tma_timeout(stntt_ctx *ctx, uint32_t spin_limit);
+
 /* ---- polynomial multiplication (pwcNtt / pwc_convolution, ntt_cpu.cpp:167-193) */
 /* d_out = cyclic convolution of d_a and d_b, length 2^log_n, i.e. the product
  * a*b mod (x^n - 1); equal to the plain product when deg a + deg b < n.

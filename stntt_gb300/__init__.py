@@ -121,6 +121,9 @@ _SIGS = {
     "stntt_batch_info": (_int, [_vp, C.POINTER(_sz), C.POINTER(_u32), C.POINTER(_sz)]),
     "stntt_batch_destroy": (_int, [_vp]),
     "stntt_selftest_wait_timeout": (_int, [_vp, _u32]),
+    "stntt_set_tma": (_int, [_vp, _int]),
+    "stntt_device_status": (_int, [_vp]),
+    "stntt_selftest_tma_timeout": (_int, [_vp, _u32]),
     "stntt_clock_s": (C.c_double, []),
     "stntt_measure_gl64_butterfly_rate": (_int, [_int, C.POINTER(C.c_double)]),
     "stntt_server_create": (_int, [_vp, C.POINTER(ServerConfig), C.POINTER(_vp)]),
@@ -301,6 +304,20 @@ class Context:
 
     def clear_plans(self) -> None:
         _check(lib().stntt_clear_plans(self._h), self._h)
+
+    def set_tma(self, mode: int) -> None:
+        """TMA-staged passes: -1 built-in choice, 0 never, 1 wherever a pass
+        allows it (stntt_set_tma; drops cached plans)."""
+        _check(lib().stntt_set_tma(self._h, mode), self._h)
+
+    def device_status(self) -> int:
+        """STNTT_ETIMEOUT (4) when a staged pass gave up waiting for a copy
+        since the last call, else 0 (stntt_device_status; synchronise first)."""
+        return lib().stntt_device_status(self._h)
+
+    def selftest_tma_timeout(self, spin_limit: int) -> int:
+        """Status of a staged launch that issues no copy (expected: 4)."""
+        return lib().stntt_selftest_tma_timeout(self._h, spin_limit)
 
     # -- device transforms (torch tensors: int32 storage for u32, int64 for gl64)
     def ntt_u32(self, data, log_n: int, batch: int, p: int, root: int, inverse: bool = False,

@@ -27,14 +27,14 @@
 namespace stntt {
 
 cudaError_t launch_tile_u32(const PassDesc &, uint32_t, const void *, const void *, void *, uint64_t, cudaStream_t,
-                             const void *);
+                             const void *, int *);
 cudaError_t launch_tile_u32l(const PassDesc &, uint32_t, const void *, const void *, void *, uint64_t, cudaStream_t,
-                             const void *);
+                             const void *, int *);
 cudaError_t batch_prepare_u32l(size_t, int *);
 cudaError_t batch_launch_u32l(const void *, const void *, unsigned long long, unsigned int *, void *, size_t, unsigned,
                               unsigned, cudaStream_t);
 cudaError_t launch_tile_gl64(const PassDesc &, uint32_t, const void *, const void *, void *, uint64_t, cudaStream_t,
-                             const void *);
+                             const void *, int *);
 cudaError_t gen_powers_u32(void *, uint64_t, uint64_t, uint64_t, uint32_t, cudaStream_t);
 cudaError_t gen_four_step_u32(void *, const void *, const void *, uint32_t, uint32_t, uint64_t, uint32_t,
                                cudaStream_t);
@@ -55,6 +55,8 @@ cudaError_t launch_cluster_gl64(const PassDesc &, const PassDesc &, uint32_t, co
                                 uint64_t, uint32_t, uint32_t, size_t, uint32_t, cudaStream_t);
 cudaError_t preload_u32l();
 cudaError_t preload_gl64();
+cudaError_t preload_tma_u32l();
+cudaError_t preload_tma_gl64();
 size_t batch_args_size_u32();
 size_t batch_args_size_gl64();
 void batch_args_fill_u32(const PassDesc &, uint32_t, const void *, const unsigned long long *,
@@ -97,16 +99,20 @@ cudaError_t preload_kernels() {
         e = preload_u32l();
     if (e == cudaSuccess)
         e = preload_gl64();
+    if (e == cudaSuccess)
+        e = preload_tma_u32l();
+    if (e == cudaSuccess)
+        e = preload_tma_gl64();
     return e;
 }
 
 cudaError_t launch_tile(int field, const PassDesc &d, uint32_t p, const void *tables, const void *in, void *out,
-                        uint64_t batch, cudaStream_t s, const void *in2) {
+                        uint64_t batch, cudaStream_t s, const void *in2, int *err) {
     if (field == kFieldGL)
-        return launch_tile_gl64(d, p, tables, in, out, batch, s, in2);
+        return launch_tile_gl64(d, p, tables, in, out, batch, s, in2, err);
     // lazy reduction needs 4p < 2^32
-    return p < (1u << 30) ? launch_tile_u32l(d, p, tables, in, out, batch, s, in2)
-                          : launch_tile_u32(d, p, tables, in, out, batch, s, in2);
+    return p < (1u << 30) ? launch_tile_u32l(d, p, tables, in, out, batch, s, in2, err)
+                          : launch_tile_u32(d, p, tables, in, out, batch, s, in2, err);
 }
 cudaError_t launch_gen_powers(int field, void *out, uint64_t count, uint64_t base, uint64_t scale, uint32_t p,
                               cudaStream_t s) {
@@ -232,6 +238,8 @@ struct stntt_ctx {
     std::string err;
     size_t mem = 0;
     uint32_t cluster_log = 3;  // log2 of the cluster size the one-launch transforms use (3 or 4)
+    int tma_mode = -1;         // TMA-staged passes: -1 built-in choice, 0 never, 1 wherever a pass allows
+    int *d_err = nullptr;      // device error word of the staged kernels' bounded waits
 };
 
 namespace sd {
@@ -335,6 +343,14 @@ void shape_pass(PassDesc &d, int field, uint64_t col_limit, uint32_t want_E, uin
     d.smem_bytes = (size_t)C * d.cs * (field == kFieldGL ? 8 : 4);
 }
 
+// Whether a pass runs TMA-staged (tma.cuh) by default; the kernel still
+// falls back to the plain one where the pass does not allow it.
+uint32_t tma_builtin(int field, const PassDesc &d) {
+    (void)field;
+    (void)d;
+    return 0;
+}
+
 // Build the pass list and the twiddle tables for one transform.
 int build_plan(stntt_ctx *ctx, Plan &pl, int field, uint32_t log_n, uint32_t p, uint64_t root_dir, int dir,
                const PlanSpec *spec) {
@@ -426,6 +442,7 @@ int build_plan(stntt_ctx *ctx, Plan &pl, int field, uint32_t log_n, uint32_t p, 
             col_limit = 1ull << 20;
         }
         shape_pass(d, field, col_limit, spec ? spec->elems[i] : 0, spec ? spec->cols[i] : 0);
+        d.tma = ctx->tma_mode < 0 ? tma_builtin(field, d) : (uint32_t)ctx->tma_mode;
         pl.passes.push_back(d);
         done += d.logL;
     }
@@ -630,7 +647,8 @@ int run_plan(stntt_ctx *ctx, const Plan &pl, const void *in, void *out, uint64_t
     }
     for (size_t i = 0; i < K; ++i) {
         void *dst = (i + 1 == K) ? out : ws;
-        cudaError_t e = launch_tile(pl.field, pl.passes[i], pl.p, pl.d_tables, src, dst, batch, s, i == 0 ? in2 : nullptr);
+        cudaError_t e = launch_tile(pl.field, pl.passes[i], pl.p, pl.d_tables, src, dst, batch, s, i == 0 ? in2 : nullptr,
+                                    ctx->d_err);
         if (e != cudaSuccess)
             return cuda_fail(ctx, e, "tile kernel launch");
         src = dst;
@@ -737,6 +755,16 @@ int host_stage(stntt_ctx *ctx, size_t bytes, void **ptr) {
 
 int ctx_device(const stntt_ctx *ctx) { return ctx->device; }
 
+// Drop every cached plan (caller holds ctx->mu; the device is idle).
+void drop_plans(stntt_ctx *ctx) {
+    for (auto &kv : ctx->plans) {
+        if (kv.second->d_tables)
+            cudaFree(kv.second->d_tables);
+        ctx->mem -= kv.second->table_bytes;
+    }
+    ctx->plans.clear();
+}
+
 void release_workspace(stntt_ctx *ctx, cudaStream_t s) {
     std::lock_guard<std::mutex> g(ctx->mu);
     auto it = ctx->workspaces.find(s);
@@ -791,10 +819,19 @@ int stntt_init(stntt_ctx **out, int device) {
     }
     if (cluster_max_size() >= 16)
         ctx->cluster_log = kClusterLogLarge;
+    if (cudaMalloc(&ctx->d_err, sizeof(int)) != cudaSuccess || cudaMemset(ctx->d_err, 0, sizeof(int)) != cudaSuccess) {
+        if (ctx->d_err)
+            cudaFree(ctx->d_err);
+        cudaStreamDestroy(ctx->setup);
+        cudaStreamDestroy(ctx->host_stream);
+        delete ctx;
+        return STNTT_ENOMEM;
+    }
     // Load every kernel now: a lazy load at first use would stall the device
     // in the middle of a caller's stream of work. This also fails early when
     // the library holds no code for this GPU.
     if (preload_kernels() != cudaSuccess) {
+        cudaFree(ctx->d_err);
         cudaStreamDestroy(ctx->setup);
         cudaStreamDestroy(ctx->host_stream);
         delete ctx;
@@ -820,6 +857,8 @@ int stntt_destroy(stntt_ctx *ctx) {
             cudaFree(kv.second.ptr);
     if (ctx->host_stage.ptr)
         cudaFree(ctx->host_stage.ptr);
+    if (ctx->d_err)
+        cudaFree(ctx->d_err);
     if (ctx->setup)
         cudaStreamDestroy(ctx->setup);
     if (ctx->host_stream)
@@ -1045,13 +1084,48 @@ int stntt_clear_plans(stntt_ctx *ctx) {
     cudaDeviceSynchronize();
     std::lock_guard<std::mutex> lk(ctx->mu);
     ctx->specs.clear();
-    for (auto &kv : ctx->plans) {
-        if (kv.second->d_tables)
-            cudaFree(kv.second->d_tables);
-        ctx->mem -= kv.second->table_bytes;
-    }
-    ctx->plans.clear();
+    drop_plans(ctx);
     return STNTT_OK;
+}
+
+int stntt_set_tma(stntt_ctx *ctx, int mode) {
+    if (!ctx || mode < -1 || mode > 1)
+        return STNTT_EINVAL;
+    DeviceGuard g(ctx->device);
+    cudaDeviceSynchronize();
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (ctx->tma_mode != mode) {
+        ctx->tma_mode = mode;
+        drop_plans(ctx);
+    }
+    return STNTT_OK;
+}
+
+int stntt_device_status(stntt_ctx *ctx) {
+    if (!ctx)
+        return STNTT_EINVAL;
+    DeviceGuard g(ctx->device);
+    int flag = 0;
+    cudaError_t e = cudaMemcpy(&flag, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && flag)
+        e = cudaMemset(ctx->d_err, 0, sizeof(int));
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "reading the device error word");
+    if (flag)
+        return fail(ctx, STNTT_ETIMEOUT, "a TMA-staged pass gave up waiting for its copy (its output is incomplete)");
+    return STNTT_OK;
+}
+
+int stntt_selftest_tma_timeout(stntt_ctx *ctx, uint32_t spin_limit) {
+    if (!ctx || spin_limit == 0)
+        return STNTT_EINVAL;
+    DeviceGuard g(ctx->device);
+    cudaError_t e = launch_tma_selftest(ctx->d_err, spin_limit, ctx->setup);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(ctx->setup);
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "TMA wait self-test");
+    return stntt_device_status(ctx);
 }
 
 int stntt_ntt_u32_oop(stntt_ctx *ctx, const uint32_t *d_in, uint32_t *d_out, uint32_t log_n, uint32_t batch,

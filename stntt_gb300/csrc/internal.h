@@ -30,11 +30,19 @@ struct PassDesc {
     uint64_t full_off = ~0ull;  // COL: w_M^(col*pos) for every (pos, col), laid out like the data; ~0 = none
     uint64_t wR[8] = {};      // raw twiddle entries (u32: {w, w'} packed little-endian)
     uint64_t scale = 0;       // raw twiddle entry
+    uint32_t tma = 0;         // 1: run as the TMA-staged persistent kernel where the pass allows it (tma.cuh)
 };
 
 // ---- launchers (return the CUDA error of the launch) ----------------------
+// err: the context's device error word; the TMA-staged kernel (tma.cuh) runs
+// only when it is given (its bounded waits report there).
 cudaError_t launch_tile(int field, const PassDesc &d, uint32_t p, const void *tables, const void *in, void *out,
-                        uint64_t batch, cudaStream_t s, const void *in2 = nullptr);
+                        uint64_t batch, cudaStream_t s, const void *in2 = nullptr, int *err = nullptr);
+// The TMA-staged kernel with no copy issued, so that its first wait runs out
+// after spin_limit polls and sets *err (self-test of the bounded wait).
+cudaError_t launch_tma_selftest(int *err, uint32_t spin_limit, cudaStream_t s);
+// Polls of an mbarrier before the TMA-staged kernel gives up (about a second).
+constexpr uint32_t kTmaSpinLimit = 1u << 22;
 // out[i] = scale * base^i, i < count, as twiddle entries (u32: Shoup pairs).
 cudaError_t launch_gen_powers(int field, void *out, uint64_t count, uint64_t base, uint64_t scale, uint32_t p,
                               cudaStream_t s);

@@ -3,6 +3,7 @@
 #pragma once
 #include <cstdlib>
 #include <cstring>
+#include <type_traits>
 #include <utility>
 
 #include "batch.cuh"
@@ -165,9 +166,27 @@ void fill_args(TileArgs<F> &a, const PassDesc &d, uint32_t p, const void *tables
     a.total = 0;
 }
 
+// The TMA-staged persistent kernel (tma.cuh) for one pass, defined per field
+// in kernels_tma_*.cu; cudaErrorNotSupported when the pass cannot use it
+// (then the plain kernel runs).
+cudaError_t launch_tma_gl64(const PassDesc &d, const TileArgs<FieldGL> &a, uint64_t batch, uint64_t tiles, int *err,
+                            cudaStream_t s);
+cudaError_t launch_tma_u32l(const PassDesc &d, const TileArgs<FieldU32L> &a, uint64_t batch, uint64_t tiles,
+                            int *err, cudaStream_t s);
+template <class F>
+cudaError_t launch_tma(const PassDesc &d, const TileArgs<F> &a, uint64_t batch, uint64_t tiles, int *err,
+                       cudaStream_t s) {
+    if constexpr (std::is_same_v<F, FieldGL>)
+        return launch_tma_gl64(d, a, batch, tiles, err, s);
+    else if constexpr (std::is_same_v<F, FieldU32L>)
+        return launch_tma_u32l(d, a, batch, tiles, err, s);
+    else
+        return cudaErrorNotSupported;
+}
+
 template <class F>
 cudaError_t launch_tile_t(const PassDesc &d, uint32_t p, const void *tables, const void *in, void *out,
-                          uint64_t batch, cudaStream_t s, const void *in2 = nullptr) {
+                          uint64_t batch, cudaStream_t s, const void *in2 = nullptr, int *err = nullptr) {
     TileArgs<F> a;
     fill_args<F>(a, d, p, tables, in, out);
     a.in2 = static_cast<const typename F::T *>(in2);
@@ -178,6 +197,11 @@ cudaError_t launch_tile_t(const PassDesc &d, uint32_t p, const void *tables, con
         return cudaSuccess;
     if (blocks > 0x7fffffffull)
         return cudaErrorInvalidConfiguration;
+    if (d.tma && err && !in2) {
+        const cudaError_t e = launch_tma<F>(d, a, batch, blocks, err, s);
+        if (e != cudaErrorNotSupported)
+            return e;
+    }
     const uint32_t tail = d.logL & 3;
     if (in2) {  // fused pointwise product: instantiated for up to 16 elements per thread
         switch (d.E) {

@@ -33,8 +33,8 @@ __global__ void fill_uniform_gl64_kernel(uint64_t *out, size_t count, uint64_t s
 }
 
 cudaError_t launch_tile_gl64(const PassDesc &d, uint32_t p, const void *tables, const void *in, void *out,
-                    uint64_t batch, cudaStream_t s, const void *in2) {
-    return launch_tile_t<FieldGL>(d, p, tables, in, out, batch, s, in2);
+                    uint64_t batch, cudaStream_t s, const void *in2, int *err) {
+    return launch_tile_t<FieldGL>(d, p, tables, in, out, batch, s, in2, err);
 }
 
 cudaError_t gen_powers_gl64(void *out, uint64_t count, uint64_t base, uint64_t scale, cudaStream_t s) {

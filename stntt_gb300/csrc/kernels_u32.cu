@@ -82,8 +82,8 @@ cudaError_t launch_stage_u32(const void *in, void *out, const void *tw, uint32_t
 }
 
 cudaError_t launch_tile_u32(const PassDesc &d, uint32_t p, const void *tables, const void *in, void *out,
-                    uint64_t batch, cudaStream_t s, const void *in2) {
-    return launch_tile_t<FieldU32>(d, p, tables, in, out, batch, s, in2);
+                    uint64_t batch, cudaStream_t s, const void *in2, int *err) {
+    return launch_tile_t<FieldU32>(d, p, tables, in, out, batch, s, in2, err);
 }
 
 cudaError_t gen_powers_u32(void *out, uint64_t count, uint64_t base, uint64_t scale, uint32_t p, cudaStream_t s) {

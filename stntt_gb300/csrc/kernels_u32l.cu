@@ -5,8 +5,8 @@
 namespace stntt {
 
 cudaError_t launch_tile_u32l(const PassDesc &d, uint32_t p, const void *tables, const void *in, void *out,
-                    uint64_t batch, cudaStream_t s, const void *in2) {
-    return launch_tile_t<FieldU32L>(d, p, tables, in, out, batch, s, in2);
+                    uint64_t batch, cudaStream_t s, const void *in2, int *err) {
+    return launch_tile_t<FieldU32L>(d, p, tables, in, out, batch, s, in2, err);
 }
 cudaError_t batch_prepare_u32l(size_t smem, int *blocks_per_sm) { return batch_prepare_t<FieldU32L>(smem, blocks_per_sm); }
 cudaError_t batch_launch_u32l(const void *args, const void *items, unsigned long long nitems, unsigned int *counters,
