@@ -71,6 +71,12 @@ int stntt_mem_usage(const stntt_ctx *ctx, size_t *bytes);
 /* findParams(size, min_mod) -> (root, mod): src/ntt/ntt_util.cpp:10-14
  * (findModulus :16-27, findPrimitiveRoot :29-34, findGenerator :36-42). */
 int stntt_find_params(uint64_t size, uint64_t min_mod, uint64_t *root, uint64_t *mod);
+/* The same search on the device, asynchronous on `stream`, for moduli below
+ * 2^32: writes d_out[0] = root, d_out[1] = mod, d_out[2] = status (STNTT_OK,
+ * or STNTT_EUNSUPPORTED when no prime k*size + 1 >= min_mod lies below 2^32).
+ * No host round trip, so parameters can be produced inside a CUDA graph.
+ * Returns STNTT_EUNSUPPORTED for size or min_mod >= 2^32. */
+int stntt_find_params_device(uint64_t size, uint64_t min_mod, uint64_t *d_out, stntt_stream stream);
 /* findParams(2^log_n, 11), the call every reference caller makes
  * (src/main.cu:37, src/bench.cu:35, src/tests/cuda/ntt/st_ntt_test.cu:20). */
 int stntt_params_u32(uint32_t log_n, uint32_t *p, uint32_t *root);

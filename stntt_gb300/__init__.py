@@ -90,6 +90,7 @@ _SIGS = {
     "stntt_last_error": (C.c_char_p, [_vp]),
     "stntt_mem_usage": (_int, [_vp, C.POINTER(_sz)]),
     "stntt_find_params": (_int, [_u64, _u64, C.POINTER(_u64), C.POINTER(_u64)]),
+    "stntt_find_params_device": (_int, [_u64, _u64, _vp, _vp]),
     "stntt_params_u32": (_int, [_u32, C.POINTER(_u32), C.POINTER(_u32)]),
     "stntt_gl64_root": (_int, [_u32, C.POINTER(_u64)]),
     "stntt_prepare": (_int, [_vp, _int, _u32, _u32, _u32, _int]),
@@ -177,6 +178,12 @@ def findParams(size: int, min_mod: int = 11) -> tuple[int, int]:
     r, m = _u64(), _u64()
     _check(lib().stntt_find_params(size, min_mod, C.byref(r), C.byref(m)))
     return r.value, m.value
+
+
+def find_params_device(size: int, min_mod: int, out, stream=None) -> None:
+    """findParams on the device (stntt_find_params_device): writes
+    (root, mod, status) into the int64 tensor `out` (3 elements) on `stream`."""
+    _check(lib().stntt_find_params_device(size, min_mod, _ptr(out), _stream(stream)))
 
 
 def params_u32(log_n: int) -> tuple[int, int]:

@@ -48,6 +48,7 @@ cudaError_t fill_uniform_gl64(void *, size_t, uint64_t, cudaStream_t);
 cudaError_t copy_scale_u32(const void *, void *, size_t, uint64_t, uint32_t, cudaStream_t);
 cudaError_t copy_scale_gl64(const void *, void *, size_t, uint64_t, cudaStream_t);
 cudaError_t launch_gl_probe(uint64_t *, unsigned, int, cudaStream_t);
+cudaError_t launch_find_params(uint64_t, uint64_t, uint64_t *, cudaStream_t);
 cudaError_t preload_u32();
 cudaError_t launch_cluster_u32l(const PassDesc &, const PassDesc &, uint32_t, const void *, const void *, void *,
                                 uint64_t, uint32_t, uint32_t, size_t, uint32_t, cudaStream_t);
@@ -909,6 +910,14 @@ int stntt_find_params(uint64_t size, uint64_t min_mod, uint64_t *root, uint64_t 
     *mod = m;
     *root = host_pow_mod(g, tot / size, m);
     return STNTT_OK;
+}
+
+int stntt_find_params_device(uint64_t size, uint64_t min_mod, uint64_t *d_out, stntt_stream stream) {
+    if (!d_out || size == 0 || min_mod == 0)
+        return STNTT_EINVAL;
+    if (size >= (1ull << 32) || min_mod >= (1ull << 32))
+        return STNTT_EUNSUPPORTED;
+    return launch_find_params(size, min_mod, d_out, (cudaStream_t)stream) == cudaSuccess ? STNTT_OK : STNTT_ECUDA;
 }
 
 int stntt_params_u32(uint32_t log_n, uint32_t *p, uint32_t *root) {

@@ -61,6 +61,7 @@ __global__ void __launch_bounds__(1024) cluster_kernel(const TileArgs<F> a1, con
                                                        uint32_t xs) {
     using T = typename F::T;
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    pdl_enter();
     T *work = reinterpret_cast<T *>(smem_raw);
     T *xbuf = work + xoff;
     cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();

@@ -1,4 +1,5 @@
 // kernels_u32.cu -- kernels over the reference's per-size 32-bit prime field.
+#include "../../include/stntt.h"
 #include "kernels_common.cuh"
 
 namespace stntt {
@@ -123,6 +124,109 @@ cudaError_t batch_prepare_u32(size_t smem, int *blocks_per_sm) { return batch_pr
 cudaError_t batch_launch_u32(const void *args, const void *items, unsigned long long nitems, unsigned int *counters,
                              void *ctl, size_t smem, unsigned grid, unsigned spin_limit, cudaStream_t s) {
     return batch_launch_t<FieldU32>(args, items, nitems, counters, ctl, smem, grid, spin_limit, s);
+}
+
+// ---- findParams on the device ----------------------------------------------
+// The reference's parameter search (src/ntt/ntt_util.cpp:10-49) for moduli
+// below 2^32, in one CTA: the smallest prime p = k size + 1 >= min_mod
+// (k >= 1; candidates tested blockDim.x at a time by trial division), the
+// smallest generator g of Z_p^* (g^((p-1)/q) != 1 for every prime q | p - 1,
+// tested blockDim.x at a time), root = g^((p-1)/size). out = {root, p,
+// status}. Every loop ends: the prime search when the next candidate reaches
+// 2^32 (status STNTT_EUNSUPPORTED), the generator search at g = p.
+__device__ __forceinline__ uint64_t fp_powmod(uint64_t b, uint64_t e, uint64_t m) {
+    uint64_t r = 1 % m;
+    b %= m;
+    while (e) {
+        if (e & 1)
+            r = r * b % m;  // m < 2^32: products fit 64 bits
+        b = b * b % m;
+        e >>= 1;
+    }
+    return r;
+}
+
+__device__ bool fp_is_prime(uint64_t n) {
+    if (n < 2)
+        return n == 1;
+    for (uint64_t x = 2; x * x <= n; ++x)
+        if (n % x == 0)
+            return false;
+    return true;
+}
+
+__global__ void __launch_bounds__(256) find_params_kernel(uint64_t size, uint64_t min_mod, uint64_t *out) {
+    __shared__ unsigned long long best;
+    __shared__ uint64_t fac[32];
+    __shared__ int nfac;
+    constexpr uint64_t kLimit = 1ull << 32;
+    const uint64_t k0 = max((min_mod - 1 + size - 1) / size, (uint64_t)1);
+    uint64_t m = 0;
+    for (uint64_t base = k0;; base += blockDim.x) {
+        if (threadIdx.x == 0)
+            best = ~0ull;
+        __syncthreads();
+        const uint64_t k = base + threadIdx.x;
+        if (k < kLimit && k * size + 1 < kLimit && fp_is_prime(k * size + 1))
+            atomicMin(&best, (unsigned long long)k);
+        __syncthreads();
+        const unsigned long long b = best;
+        if (b != ~0ull) {
+            m = b * size + 1;
+            break;
+        }
+        if (base + blockDim.x >= kLimit || (base + blockDim.x) * size + 1 >= kLimit) {
+            if (threadIdx.x == 0) {
+                out[0] = 0;
+                out[1] = 0;
+                out[2] = STNTT_EUNSUPPORTED;
+            }
+            return;
+        }
+        __syncthreads();  // everyone has read `best` before it is reset
+    }
+    const uint64_t tot = m - 1;
+    if (threadIdx.x == 0) {
+        int nf = 0;
+        uint64_t r = tot;
+        for (uint64_t q = 2; q * q <= r; ++q)
+            if (r % q == 0) {
+                fac[nf++] = q;
+                while (r % q == 0)
+                    r /= q;
+            }
+        if (r > 1)
+            fac[nf++] = r;
+        nfac = nf;
+        best = ~0ull;
+    }
+    __syncthreads();
+    for (uint64_t base = 1; base < m; base += blockDim.x) {
+        const uint64_t c = base + threadIdx.x;
+        if (c < m && fp_powmod(c, tot, m) == 1 % m) {
+            bool ok = true;
+            for (int i = 0; i < nfac && ok; ++i)
+                ok = fp_powmod(c, tot / fac[i], m) != 1;
+            if (ok)
+                atomicMin(&best, (unsigned long long)c);
+        }
+        __syncthreads();
+        const unsigned long long b = best;
+        if (b != ~0ull)
+            break;
+        __syncthreads();  // everyone has read `best` before the next candidates
+    }
+    if (threadIdx.x == 0) {
+        const uint64_t g = best;
+        out[0] = g == ~0ull ? 0 : fp_powmod(g, tot / size, m);
+        out[1] = g == ~0ull ? 0 : m;
+        out[2] = g == ~0ull ? STNTT_EUNSUPPORTED : STNTT_OK;
+    }
+}
+
+cudaError_t launch_find_params(uint64_t size, uint64_t min_mod, uint64_t *out, cudaStream_t s) {
+    find_params_kernel<<<1, 256, 0, s>>>(size, min_mod, out);
+    return cudaGetLastError();
 }
 
 cudaError_t preload_u32() {

@@ -29,6 +29,14 @@
 
 namespace stntt {
 
+// Programmatic dependent launch (no-ops for a launch without the
+// programmatic-serialization attribute): a kernel waits until the previous
+// kernel's writes are visible before it touches global memory, and lets the
+// next kernel start launching once it reaches its last step (so that the next
+// kernel's CTAs take SM slots only near the end of this one).
+__device__ __forceinline__ void pdl_enter() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 template <class F>
 struct TileArgs {
     using T = typename F::T;
@@ -148,6 +156,8 @@ __device__ __forceinline__ void tile_step(const TileArgs<F> &a, const F &f, type
     using T = typename F::T;
     constexpr int R = 1 << LOGR, ITEMS = E / R;
     const uint32_t L = 1u << a.logL, U = L / E, T_ = L >> LOGR;
+    if constexpr (last)
+        pdl_trigger();
     const uint32_t pm = (1u << logp) - 1;
     T *col_sm = sm + c * a.cs;
 
@@ -310,9 +320,11 @@ __device__ __forceinline__ void tile_run(const TileArgs<F> &a, uint64_t blk, typ
     }
 }
 
+
 template <class F, int E, int TAIL, bool IN2 = false>
 __global__ void __launch_bounds__(E >= 32 ? 512 : 1024) tile_kernel(const TileArgs<F> a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    pdl_enter();
     tile_run<F, E, TAIL, IN2>(a, blockIdx.x, reinterpret_cast<typename F::T *>(smem_raw));
 }
 
@@ -342,6 +354,8 @@ __device__ __forceinline__ void tile_step_l(const TileArgs<F> &a, const F &f, ty
     constexpr int R = 1 << LOGR, ITEMS = E / R;
     constexpr uint32_t PS = Pad<F>::PS, U = (1u << LOGL) / E, TS = (1u << LOGL) >> LOGR, P = 1u << LOGP;
     static_assert(LOGR + LOGP <= LOGL, "step beyond the tile");
+    if constexpr (last)
+        pdl_trigger();
     // ---- read R inputs per item: idx = u + m U + r L/R
     const uint32_t pu = Pad<F>::at(u);
 #pragma unroll
@@ -421,6 +435,7 @@ __device__ __forceinline__ void tile_run_l(const TileArgs<F> &a, uint64_t blk, t
 template <class F, int LOGL, bool FULL4 = false>
 __global__ void __launch_bounds__(1024) tile_kernel_l(const TileArgs<F> a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    pdl_enter();
     tile_run_l<F, LOGL, FULL4>(a, blockIdx.x, reinterpret_cast<typename F::T *>(smem_raw));
 }
 
