@@ -115,6 +115,12 @@ int stntt_set_plan(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t npasses, 
  * shape per n, src/cuda/ntt/ntt_kernel.cuh:31-39). */
 int stntt_set_plan_small(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t npasses, const uint32_t *pass_logs,
                          const uint32_t *elems, const uint32_t *cols);
+/* The pass split (1 or 2 passes, each of 2^4..2^13 points) a job of this size
+ * takes inside the persistent batched launch (stntt_batch_create,
+ * stntt_ntt_batch), whose tiles are 8192 elements with 16 per thread; tuned
+ * separately because that kernel's best split differs from a plain call's.
+ * Extends the reference's manual block-size sweep (src/bench.cu:88-91). */
+int stntt_set_plan_batched(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t npasses, const uint32_t *pass_logs);
 int stntt_clear_plans(stntt_ctx *ctx);
 /* "name|SM count|driver version|compute capability" of a device: the key
  * under which tuned plans are cached. */

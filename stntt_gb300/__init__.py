@@ -97,6 +97,7 @@ _SIGS = {
     "stntt_plan_info": (_int, [_vp, _int, _u32, _u32, _u32, _int, C.POINTER(_u32), C.POINTER(_u32)]),
     "stntt_set_plan": (_int, [_vp, _int, _u32, _u32, C.POINTER(_u32), C.POINTER(_u32), C.POINTER(_u32)]),
     "stntt_set_plan_small": (_int, [_vp, _int, _u32, _u32, C.POINTER(_u32), C.POINTER(_u32), C.POINTER(_u32)]),
+    "stntt_set_plan_batched": (_int, [_vp, _int, _u32, _u32, C.POINTER(_u32)]),
     "stntt_call_info": (_int, [_vp, _int, _u32, _u32, _u32, _u32, _int, C.POINTER(_u32), C.POINTER(_u32)]),
     "stntt_clear_plans": (_int, [_vp]),
     "stntt_device_key": (_int, [_int, C.c_char_p, _sz]),
@@ -301,11 +302,17 @@ class Context:
                                      C.byref(n), logs), self._h)
         return n.value, [v for v in logs if v]
 
-    def set_plan(self, field: int, log_n: int, pass_logs, elems=None, cols=None, small: bool = False) -> None:
+    def set_plan(self, field: int, log_n: int, pass_logs, elems=None, cols=None, small: bool = False,
+                 batched: bool = False) -> None:
         """Override the plan shape for one size (stntt_set_plan); small=True sets
-        the shape for calls of fewer than 2^22 elements (stntt_set_plan_small)."""
+        the shape for calls of fewer than 2^22 elements (stntt_set_plan_small),
+        batched=True the pass split of jobs in the persistent batched launch
+        (stntt_set_plan_batched; elems and cols do not apply there)."""
         k = len(pass_logs)
         arr = lambda v: (_u32 * k)(*(v if v is not None else [0] * k))  # noqa: E731
+        if batched:
+            _check(lib().stntt_set_plan_batched(self._h, field, log_n, k, arr(pass_logs)), self._h)
+            return
         fn = lib().stntt_set_plan_small if small else lib().stntt_set_plan
         _check(fn(self._h, field, log_n, k, arr(pass_logs), arr(elems), arr(cols)), self._h)
 

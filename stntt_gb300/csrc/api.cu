@@ -192,14 +192,18 @@ using namespace stntt;
 // ---------------------------------------------------------------------------
 namespace sd {
 
+// Elements per work item of the persistent batched launch (C columns or rows
+// of L points, 16 per thread, 512 threads).
+constexpr uint32_t kBatchTileLog = 13;
+
 struct PlanKey {
     int field;
     uint32_t log_n, p;
     uint64_t root;  // root of the direction (inverse: root^-1)
     int dir;
-    bool small;  // built from the shape set for small calls (stntt_set_plan_small)
+    int kind;  // the shape set it was built from: kPlanAll, kPlanSmall or kPlanBatched
     bool operator<(const PlanKey &o) const {
-        return std::tie(field, log_n, p, root, dir, small) < std::tie(o.field, o.log_n, o.p, o.root, o.dir, o.small);
+        return std::tie(field, log_n, p, root, dir, kind) < std::tie(o.field, o.log_n, o.p, o.root, o.dir, o.kind);
     }
 };
 
@@ -230,7 +234,7 @@ struct stntt_ctx {
     std::map<PlanKey, std::unique_ptr<Plan>> plans;
     std::map<std::tuple<uint32_t, uint32_t, uint32_t, int>, DevBuf> stage_tables;  // (log_n, p, root, wrap)
     std::map<cudaStream_t, DevBuf> workspaces;
-    std::map<std::tuple<int, uint32_t, bool>, PlanSpec> specs;  // (field, log_n, small) -> override
+    std::map<std::tuple<int, uint32_t, int>, PlanSpec> specs;  // (field, log_n, kind) -> override
     cudaStream_t setup = nullptr;
     // host-buffer calls: one at a time, on their own stream and staging buffer
     std::mutex host_mu;
@@ -471,12 +475,14 @@ int build_plan(stntt_ctx *ctx, Plan &pl, int field, uint32_t log_n, uint32_t p, 
 }
 
 int get_plan(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t p, uint64_t root, int dir, const Plan **out,
-             bool small) {
+             int kind) {
     const uint64_t rd = dir_root(field, root, p, dir);
     std::lock_guard<std::mutex> g(ctx->mu);
-    // a small call uses the small-call shape when one is set, else the plan of every call
-    small = small && ctx->specs.count({field, log_n, true});
-    PlanKey key{field, log_n, field == kFieldGL ? 0u : p, rd, dir, small};
+    // a small call (batched launch) uses the small-call (batched) shape when
+    // one is set, else the plan of every call
+    if (kind != kPlanAll && !ctx->specs.count({field, log_n, kind}))
+        kind = kPlanAll;
+    PlanKey key{field, log_n, field == kFieldGL ? 0u : p, rd, dir, kind};
     auto it = ctx->plans.find(key);
     if (it != ctx->plans.end()) {
         *out = it->second.get();
@@ -484,7 +490,7 @@ int get_plan(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t p, uint64_t roo
     }
     auto pl = std::make_unique<Plan>();
     PlanSpec spec;
-    auto sit = ctx->specs.find({field, log_n, small});
+    auto sit = ctx->specs.find({field, log_n, kind});
     const bool has_spec = sit != ctx->specs.end();
     if (has_spec)
         spec = sit->second;
@@ -986,8 +992,8 @@ int stntt_plan_info(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t p, uint3
 namespace {
 
 int set_plan_for(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t npasses, const uint32_t *pass_logs,
-                 const uint32_t *elems, const uint32_t *cols, bool small) {
-    if (!ctx || !pass_logs || npasses == 0 || npasses > 3)
+                 const uint32_t *elems, const uint32_t *cols, int kind) {
+    if (!ctx || !pass_logs || npasses == 0 || npasses > (kind == kPlanBatched ? 2u : 3u))
         return fail(ctx, STNTT_EINVAL, "set_plan: bad arguments");
     if (field != STNTT_FIELD_U32 && field != STNTT_FIELD_GL64)
         return fail(ctx, STNTT_EINVAL, "set_plan: unknown field");
@@ -1012,7 +1018,7 @@ int set_plan_for(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t npasses, co
     DeviceGuard g(ctx->device);
     cudaDeviceSynchronize();  // plans about to be freed may be in use
     std::lock_guard<std::mutex> lk(ctx->mu);
-    ctx->specs[{f, log_n, small}] = s;
+    ctx->specs[{f, log_n, kind}] = s;
     for (auto it = ctx->plans.begin(); it != ctx->plans.end();) {
         if (it->first.field == f && it->first.log_n == log_n) {
             if (it->second->d_tables)
@@ -1066,12 +1072,23 @@ int stntt_call_info(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t batch, u
 
 int stntt_set_plan(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t npasses, const uint32_t *pass_logs,
                    const uint32_t *elems, const uint32_t *cols) {
-    return set_plan_for(ctx, field, log_n, npasses, pass_logs, elems, cols, false);
+    return set_plan_for(ctx, field, log_n, npasses, pass_logs, elems, cols, kPlanAll);
 }
 
 int stntt_set_plan_small(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t npasses, const uint32_t *pass_logs,
                          const uint32_t *elems, const uint32_t *cols) {
-    return set_plan_for(ctx, field, log_n, npasses, pass_logs, elems, cols, true);
+    return set_plan_for(ctx, field, log_n, npasses, pass_logs, elems, cols, kPlanSmall);
+}
+
+int stntt_set_plan_batched(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t npasses, const uint32_t *pass_logs) {
+    if (npasses == 1 && pass_logs && pass_logs[0] < 4)
+        return fail(ctx, STNTT_EINVAL, "set_plan_batched: passes must be at least 2^4 points");
+    if (npasses == 2 && pass_logs && (pass_logs[0] < 4 || pass_logs[1] < 4))
+        return fail(ctx, STNTT_EINVAL, "set_plan_batched: passes must be at least 2^4 points");
+    // a work item of a two-pass job holds 8192 elements of that one job
+    if (npasses == 2 && log_n < kBatchTileLog)
+        return fail(ctx, STNTT_EINVAL, "set_plan_batched: two passes need at least 2^13 points");
+    return set_plan_for(ctx, field, log_n, npasses, pass_logs, nullptr, nullptr, kPlanBatched);
 }
 
 int stntt_device_key(int device, char *buf, size_t len) {
@@ -1518,7 +1535,7 @@ void args_fill(int field, const PassDesc &d, uint32_t p, const void *t, const un
 void batch_shape(PassDesc &d, int field) {
     const uint32_t L = 1u << d.logL;
     d.E = 16;
-    const uint32_t U = L / 16, C = 8192 / L;
+    const uint32_t U = L / 16, C = (1u << kBatchTileLog) / L;
     d.logC = ilog2(C);
     d.threads = C * U;
     d.cs = column_stride(field, L, C, U, d.tfast);
@@ -1572,7 +1589,7 @@ int build_part(stntt_ctx *ctx, stntt_batch *bt, int field, const std::vector<con
         uint64_t root = ck.root;
         if (field == kFieldGL)
             stntt_gl64_root(ck.log_n, &root);
-        int rc = get_plan(ctx, field, ck.log_n, ck.p, root, (int)ck.dir, &pl);
+        int rc = get_plan(ctx, field, ck.log_n, ck.p, root, (int)ck.dir, &pl, kPlanBatched);
         if (rc)
             return rc;
         const size_t J = cj.size();
@@ -1704,13 +1721,15 @@ int stntt_batch_create(stntt_ctx *ctx, const stntt_job *jobs, size_t njobs, stnt
             uint64_t root = j.root;
             if (f == kFieldGL)
                 stntt_gl64_root(j.log_n, &root);
-            int rc = get_plan(ctx, f, j.log_n, f == kFieldGL ? 0 : j.p, root, (int)j.dir, &pl);
+            int rc = get_plan(ctx, f, j.log_n, f == kFieldGL ? 0 : j.p, root, (int)j.dir, &pl, kPlanBatched);
             if (rc)
                 return rc;
             passes = (uint32_t)pl->passes.size();
             for (const PassDesc &d : pl->passes)
                 if (d.logL < 4)
                     passes = 99;  // the persistent kernel's tiles are at least 16 long
+            if (passes == 2 && j.log_n < kBatchTileLog)
+                passes = 99;  // a two-pass work item holds 8192 elements of one job
             if (passes == 2)
                 scratch_need = ((size_t)1 << j.log_n) * (f == kFieldGL ? 8 : 4);
         }

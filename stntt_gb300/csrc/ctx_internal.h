@@ -13,11 +13,14 @@ namespace sd {
 struct Plan;
 
 // Twiddle tables and pass list for one transform (built and cached on first use).
-// small: the call transforms fewer than kSmallCallElems elements in all (it
-// uses the small-call shape when stntt_set_plan_small set one).
+// kind: kPlanSmall for a call of fewer than kSmallCallElems elements in all,
+// kPlanBatched for a job of the persistent batched launch; each uses its own
+// shape when stntt_set_plan_small / stntt_set_plan_batched set one, else the
+// shape of every call (kPlanAll).
 constexpr uint64_t kSmallCallElems = 1ull << 22;
+enum : int { kPlanAll = 0, kPlanSmall = 1, kPlanBatched = 2 };
 int get_plan(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t p, uint64_t root, int dir, const Plan **out,
-             bool small = false);
+             int kind = kPlanAll);
 // Run a plan: first pass reads `in`, last pass writes `out`, on stream s.
 // in2: optional second input whose product with `in` the first pass transforms.
 int run_plan(stntt_ctx *ctx, const Plan &pl, const void *in, void *out, uint64_t batch, cudaStream_t s,

@@ -1,4 +1,5 @@
-"""Autotuner for transform plans: pass split, elements per thread, columns per CTA.
+"""Autotuner for transform plans: pass split, elements per thread, columns per CTA
+(and, with --batched, the pass split of jobs in the persistent batched launch).
 
 For one (field, log_n) it enumerates plan shapes the library accepts
 (``stntt_set_plan``), times each forward transform with CUDA events on a
@@ -123,6 +124,79 @@ def tune(ctx: st.Context, field: int, log_n: int, reps: int = 10, full: bool = F
     return best, results
 
 
+def batched_candidates(log_n: int) -> list[list[int]]:
+    """Pass splits a job can take inside the persistent batched launch: one
+    pass, or (from 2^13 points: a work item holds 8192 elements of one job)
+    two of 2^4..2^13 points each."""
+    out = [[log_n]] if 4 <= log_n <= 13 else []
+    if log_n >= 13:
+        for a in range(4, 14):
+            if 4 <= log_n - a <= 13:
+                out.append([a, log_n - a])
+    return out
+
+
+def tune_batched(ctx: st.Context, field: int, log_n: int, reps: int = 10, verbose: bool = False, jobs: int = 0):
+    """Pass split for jobs of one size in the persistent batched launch: times
+    stntt_batch_launch (captured in a CUDA graph and replayed, as in the bench's
+    uneven mix) on `jobs` same-size transforms, half forward and half inverse,
+    2^25 elements in all by default (more than L2 holds). Returns (best, all
+    results) and leaves the best split set."""
+    import torch
+
+    jobs = jobs or max(8, (1 << 25) >> log_n)
+    n = 1 << log_n
+    dev = f"cuda:{ctx.device}"
+    if field == st.FIELD_GL64:
+        data = torch.empty(jobs * n, dtype=torch.int64, device=dev)
+        st.fill_uniform_gl64(data, 98)
+        p = root = 0
+        esz = 8
+    else:
+        p, root = st.params_u32(log_n)
+        data = torch.empty(jobs * n, dtype=torch.int32, device=dev)
+        st.fill_uniform_u32(data, 98, p)
+        esz = 4
+    job_list = [st.Job(field, log_n, i % 2, p, root, 0, data.data_ptr() + esz * n * i) for i in range(jobs)]
+    stream = torch.cuda.Stream(device=dev)
+    results = []
+    for logs in batched_candidates(log_n):
+        try:
+            ctx.set_plan(field, log_n, logs, batched=True)
+            b = ctx.batch_create(job_list)
+        except st.StnttError as e:
+            if verbose:
+                print("skip", logs, e)
+            continue
+        try:
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=stream):
+                b.launch(stream=stream)
+            for _ in range(2):
+                g.replay()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                g.replay()
+            e1.record()
+            torch.cuda.synchronize()
+            ok = b.status() == 0
+        finally:
+            b.close()
+        if not ok:
+            continue
+        us = e0.elapsed_time(e1) * 1e3 / reps
+        results.append({"logs": logs, "E": [16] * len(logs), "C": [0] * len(logs), "us": us, "batch": jobs,
+                        "batched": True})
+        if verbose:
+            print(f"batched {logs}: {us:.1f} us", flush=True)
+    results.sort(key=lambda r: r["us"])
+    best = results[0]
+    ctx.set_plan(field, log_n, best["logs"], batched=True)
+    return best, results
+
+
 def _key(device: int) -> str:
     return st.device_key(device)
 
@@ -154,9 +228,12 @@ def apply_cache(ctx: st.Context, path: Path = DEFAULT_CACHE) -> int:
     entries.update(load_cache(path).get(key, {}))
     k = 0
     for name, e in entries.items():
-        parts = name.split(":")  # "field:log_n", or "field:log_n:b1" for single-transform calls
+        # "field:log_n", "field:log_n:b1" for single-transform calls, "field:log_n:batch"
+        # for jobs of the persistent batched launch
+        parts = name.split(":")
         field = st.FIELD_GL64 if parts[0] == "gl64" else st.FIELD_U32
-        ctx.set_plan(field, int(parts[1]), e["logs"], e["E"], e["C"], small=len(parts) > 2)
+        tag = parts[2] if len(parts) > 2 else ""
+        ctx.set_plan(field, int(parts[1]), e["logs"], e["E"], e["C"], small=tag == "b1", batched=tag == "batch")
         k += 1
     return k
 
@@ -167,7 +244,8 @@ def record(ctx: st.Context, field: int, log_n: int, best: dict, path: Path = DEF
     cache = load_cache(path)
     ent = cache.setdefault(_key(ctx.device), {})
     small = (best["batch"] << log_n) < (1 << 22)
-    ent[f"{'gl64' if field == st.FIELD_GL64 else 'u32'}:{log_n}" + (":b1" if small else "")] = {
+    suffix = ":batch" if best.get("batched") else (":b1" if small else "")
+    ent[f"{'gl64' if field == st.FIELD_GL64 else 'u32'}:{log_n}" + suffix] = {
         "logs": best["logs"], "E": best["E"], "C": best["C"], "us": best["us"], "batch": best["batch"],
         "when": time.strftime("%Y-%m-%dT%H:%M:%SZ", time.gmtime())}
     save_cache(cache, path)
@@ -195,11 +273,19 @@ def main() -> None:
     ap.add_argument("--verbose", action="store_true")
     ap.add_argument("--out", default=None, help="also write all timings here (JSON)")
     ap.add_argument("--package", action="store_true", help="fold the results into the packaged plans")
+    ap.add_argument("--batched", action="store_true",
+                    help="tune the pass split of jobs in the persistent batched launch instead")
     args = ap.parse_args()
     field = st.FIELD_GL64 if args.field == "gl64" else st.FIELD_U32
     ctx = st.Context(0)
     allres = {}
     for lg in args.log_n:
+        if args.batched:
+            best, res = tune_batched(ctx, field, lg, args.reps, args.verbose, args.batch)
+            record(ctx, field, lg, best, Path(args.cache))
+            allres[f"{args.field}:{lg}:batch"] = res
+            print(json.dumps({"size": f"{args.field}:{lg}:batch", "best": best, "candidates": len(res)}), flush=True)
+            continue
         best, res = tune(ctx, field, lg, args.reps, args.full, args.verbose, args.batch)
         record(ctx, field, lg, best, Path(args.cache))
         allres[f"{args.field}:{lg}" + (":b1" if (best["batch"] << lg) < (1 << 22) else "")] = res

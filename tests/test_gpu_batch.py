@@ -110,3 +110,33 @@ def test_bounded_wait_reports_timeout(ctx):
     ctx.ntt_gl64(d, 12)
     torch.cuda.synchronize()
     assert np.array_equal(_host(d), O.ntt_gl64(x))
+
+
+def test_batched_plan_splits(ctx):
+    """stntt_set_plan_batched: jobs of the persistent launch take the split set
+    for their size (one pass, or from 2^13 points two of 2^4..2^13 points,
+    including uneven ones), bit-exact with the oracle."""
+    splits = {12: [12], 13: [4, 9], 14: [9, 5], 16: [5, 11], 17: [7, 10], 18: [7, 11]}
+    try:
+        for lg, sp in splits.items():
+            ctx.set_plan(st.FIELD_GL64, lg, sp, batched=True)
+            ctx.set_plan(st.FIELD_U32, lg, sp, batched=True)
+        jobs, bufs, inputs, meta = _make_jobs(11, 40, 12, 18)
+        b = ctx.batch_create(jobs)
+        assert b.info()["fallback_jobs"] == 0
+        b.launch()
+        torch.cuda.synchronize()
+        assert b.status() == 0
+        for d, x, m in zip(bufs, inputs, meta):
+            assert np.array_equal(_host(d), _expected(x, m)), m
+        b.close()
+        with pytest.raises(st.StnttError):
+            ctx.set_plan(st.FIELD_GL64, 20, [4, 8, 8], batched=True)  # three passes: not in the persistent launch
+        with pytest.raises(st.StnttError):
+            ctx.set_plan(st.FIELD_GL64, 14, [2, 12], batched=True)  # tiles below 2^4 points
+        with pytest.raises(st.StnttError):
+            ctx.set_plan(st.FIELD_GL64, 12, [6, 6], batched=True)  # two passes below 2^13 points
+    finally:
+        ctx.clear_plans()
+        from stntt_gb300 import tune
+        tune.apply_cache(ctx)
