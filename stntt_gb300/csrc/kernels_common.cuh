@@ -83,13 +83,29 @@ cudaError_t launch_tile_e(const PassDesc &d, const TileArgs<F> &a, uint64_t bloc
 // Tile lengths 2^4..2^13 at 16 elements per thread: the kernel with the
 // length compiled in (column passes with a full four-step table from 2^6 up:
 // the FULL4 build). false when logL is outside that range.
-template <class F, int LOGL>
-cudaError_t launch_tile_l(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks, cudaStream_t s) {
+// 32-bit lazy-field passes of at most 256 threads per CTA run the build with
+// six CTAs resident per SM (at most 40 registers, no spills): 32-bit 2^26
+// forward + inverse 1354 -> 1269 us per step on GB300 (eight per SM: 1274 us,
+// with spills). Goldilocks passes keep 64 registers (five per SM spilled and
+// ran 11% slower).
+constexpr int kU32MinBlocks = 6;
+
+template <class F, int LOGL, int MINB>
+cudaError_t launch_tile_lm(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks, cudaStream_t s) {
     if constexpr (LOGL >= 6) {
         if (a.tw4_full && a.mode == kModeCol)
-            return launch_tile_k<F, tile_kernel_l<F, LOGL, true>>(d, a, blocks, s);
+            return launch_tile_k<F, tile_kernel_l<F, LOGL, true, MINB>>(d, a, blocks, s);
     }
-    return launch_tile_k<F, tile_kernel_l<F, LOGL>>(d, a, blocks, s);
+    return launch_tile_k<F, tile_kernel_l<F, LOGL, false, MINB>>(d, a, blocks, s);
+}
+
+template <class F, int LOGL>
+cudaError_t launch_tile_l(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks, cudaStream_t s) {
+    if constexpr (std::is_same_v<F, FieldU32L>) {
+        if (d.threads <= 256)
+            return launch_tile_lm<F, LOGL, kU32MinBlocks>(d, a, blocks, s);
+    }
+    return launch_tile_lm<F, LOGL, 1>(d, a, blocks, s);
 }
 
 template <class F>
@@ -393,6 +409,13 @@ cudaError_t preload_fixed_t(std::integer_sequence<int, LOGL...>) {
     ((e = (e == cudaSuccess ? tile_attr<F, tile_kernel_l<F, LOGL + 4>>() : e)), ...);
     ((e = (e == cudaSuccess && LOGL + 4 >= 6 ? tile_attr<F, tile_kernel_l<F, LOGL + 4, (LOGL + 4 >= 6)>>() : e)),
      ...);
+    if constexpr (std::is_same_v<F, FieldU32L>) {
+        ((e = (e == cudaSuccess ? tile_attr<F, tile_kernel_l<F, LOGL + 4, false, kU32MinBlocks>>() : e)), ...);
+        ((e = (e == cudaSuccess && LOGL + 4 >= 6
+                   ? tile_attr<F, tile_kernel_l<F, LOGL + 4, (LOGL + 4 >= 6), kU32MinBlocks>>()
+                   : e)),
+         ...);
+    }
     return e;
 }
 

@@ -432,8 +432,10 @@ __device__ __forceinline__ void tile_run_l(const TileArgs<F> &a, uint64_t blk, t
     tile_steps_l<F, 16, LOGL, 0, GlobalIO<F, FULL4>>(a, f, x, sm + c * a.cs, u, GlobalIO<F, FULL4>{g});
 }
 
-template <class F, int LOGL, bool FULL4 = false>
-__global__ void __launch_bounds__(1024) tile_kernel_l(const TileArgs<F> a) {
+// MINB > 1: a build for CTAs of at most 256 threads with MINB of them resident
+// per SM (registers capped at 65536 / (256 MINB) per thread).
+template <class F, int LOGL, bool FULL4 = false, int MINB = 1>
+__global__ void __launch_bounds__(MINB > 1 ? 256 : 1024, MINB) tile_kernel_l(const TileArgs<F> a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     pdl_enter();
     tile_run_l<F, LOGL, FULL4>(a, blockIdx.x, reinterpret_cast<typename F::T *>(smem_raw));
