@@ -201,9 +201,11 @@ struct PlanKey {
     uint32_t log_n, p;
     uint64_t root;  // root of the direction (inverse: root^-1)
     int dir;
-    int kind;  // the shape set it was built from: kPlanAll, kPlanSmall or kPlanBatched
+    int kind;         // the shape set it was built from: kPlanAll, kPlanSmall or kPlanBatched
+    bool small_call;  // for calls of fewer than kSmallCallElems elements (smaller full twiddle tables)
     bool operator<(const PlanKey &o) const {
-        return std::tie(field, log_n, p, root, dir, kind) < std::tie(o.field, o.log_n, o.p, o.root, o.dir, o.kind);
+        return std::tie(field, log_n, p, root, dir, kind, small_call) <
+               std::tie(o.field, o.log_n, o.p, o.root, o.dir, o.kind, o.small_call);
     }
 };
 
@@ -358,7 +360,7 @@ uint32_t tma_builtin(int field, const PassDesc &d) {
 
 // Build the pass list and the twiddle tables for one transform.
 int build_plan(stntt_ctx *ctx, Plan &pl, int field, uint32_t log_n, uint32_t p, uint64_t root_dir, int dir,
-               const PlanSpec *spec) {
+               const PlanSpec *spec, bool small_call) {
     pl.field = field;
     pl.log_n = log_n;
     pl.p = p;
@@ -435,7 +437,7 @@ int build_plan(stntt_ctx *ctx, Plan &pl, int field, uint32_t log_n, uint32_t p, 
             // one product per element instead of two lookups and two products
             // (M entries per plan; the lo / hi tables stay for the kernels
             // without this path).
-            if (d.logM >= kFullTwiddleMinLog && d.logM <= kFullTwiddleMaxLog)
+            if (d.logM >= kFullTwiddleMinLog && d.logM <= (small_call ? kFullTwiddleMaxLogSmall : kFullTwiddleMaxLog))
                 d.full_off = add_full(1ull << d.logM, d.lo_off, d.hi_off, d.h, d.logS);
             col_limit = 1ull << d.logS;
         } else {
@@ -480,9 +482,10 @@ int get_plan(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t p, uint64_t roo
     std::lock_guard<std::mutex> g(ctx->mu);
     // a small call (batched launch) uses the small-call (batched) shape when
     // one is set, else the plan of every call
+    const bool small_call = kind == kPlanSmall;
     if (kind != kPlanAll && !ctx->specs.count({field, log_n, kind}))
         kind = kPlanAll;
-    PlanKey key{field, log_n, field == kFieldGL ? 0u : p, rd, dir, kind};
+    PlanKey key{field, log_n, field == kFieldGL ? 0u : p, rd, dir, kind, small_call};
     auto it = ctx->plans.find(key);
     if (it != ctx->plans.end()) {
         *out = it->second.get();
@@ -495,7 +498,7 @@ int get_plan(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t p, uint64_t roo
     if (has_spec)
         spec = sit->second;
     ctx->mu.unlock();
-    int rc = build_plan(ctx, *pl, field, log_n, p, rd, dir, has_spec ? &spec : nullptr);
+    int rc = build_plan(ctx, *pl, field, log_n, p, rd, dir, has_spec ? &spec : nullptr, small_call);
     ctx->mu.lock();
     if (rc != STNTT_OK) {
         if (pl->d_tables)

@@ -13,8 +13,12 @@ enum : uint32_t { kModeCol = 0, kModeRow = 1 };  // tile pass kinds (tile.cuh)
 // Column passes over sub-problems of 2^14..2^20 points read their four-step
 // twiddle from a full table (at most 8 MB, so it stays in L2 across the
 // batch and the sub-problems); larger ones, whose table would stream from
-// HBM on the store path, keep the two-level lookup.
-constexpr uint32_t kFullTwiddleMinLog = 14, kFullTwiddleMaxLog = 20;
+// HBM on the store path, keep the two-level lookup. Calls of fewer than 2^22
+// elements use full tables only up to 2^17 points: a lone 2^20-point call
+// would read its 8 MB table from HBM once per call, as many bytes as its data
+// (measured on GB300, Goldilocks 2^20 forward + inverse with L2 flushed
+// between steps: 84.5 us with the full table, 77.8 us without).
+constexpr uint32_t kFullTwiddleMinLog = 14, kFullTwiddleMaxLog = 20, kFullTwiddleMaxLogSmall = 17;
 // One-launch transforms: 16-CTA clusters (non-portable size) where the device
 // schedules them, else 8; up to 2^(15 + log2 K) bytes per transform.
 constexpr uint32_t kClusterLogSmall = 3, kClusterLogLarge = 4;
