@@ -102,7 +102,7 @@ int stntt_call_info(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t batch, u
 
 /* Override the plan for one (field, log_n): npasses HBM passes (1..4) with
  * tile lengths 2^pass_logs[i] (summing to log_n, each <= 13; npasses <= 3), elements per
- * thread elems[i] (16 or 32; 0 = default) and columns per CTA cols[i] (a power
+ * thread elems[i] (16 or 32, or 8 for tiles of 2^7..2^11 points; 0 = default) and columns per CTA cols[i] (a power
  * of two; 0 = default). Drops cached plans of that size. The autotuner
  * (stntt_gb300/tune.py) drives this and stores its choices on disk.
  * stntt_clear_plans() restores the built-in defaults for every size. */

@@ -327,6 +327,8 @@ void shape_pass(PassDesc &d, int field, uint64_t col_limit, uint32_t want_E, uin
     d.E = L < 16 ? L : 16;
     if (L >= 16 && (want_E == 16 || want_E == 32) && want_E <= L)
         d.E = want_E;
+    if (want_E == 8 && d.logL >= 7 && d.logL <= 11)  // the 8-element compile-time builds
+        d.E = 8;
     const uint32_t U = L / d.E;
     const uint32_t max_threads = d.E >= 32 ? 512 : 1024;
     uint64_t C;
@@ -648,7 +650,8 @@ int run_plan(stntt_ctx *ctx, const Plan &pl, const void *in, void *out, uint64_t
     }
     const size_t K = pl.passes.size();
     const void *src = in;
-    if (in2 && pl.passes[0].E > 16) {  // no fused kernel for this shape: separate pointwise product
+    const PassDesc &p0 = pl.passes[0];
+    if (in2 && p0.E != 16 && (1u << p0.logL) > p0.E) {  // no fused kernel for this shape: separate pointwise product
         cudaError_t e = launch_pointwise(pl.field, in, in2, out, (size_t)batch << pl.log_n, pl.p, s);
         if (e != cudaSuccess)
             return cuda_fail(ctx, e, "pointwise launch");
@@ -1006,8 +1009,8 @@ int set_plan_for(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t npasses, co
         const uint32_t lg = pass_logs[i], e = elems ? elems[i] : 0, c = cols ? cols[i] : 0;
         if (lg == 0 || lg > 13)
             return fail(ctx, STNTT_EINVAL, "set_plan: each pass length must be 2^1..2^13");
-        if (e != 0 && e != 16 && e != 32)
-            return fail(ctx, STNTT_EINVAL, "set_plan: elems must be 0, 16 or 32");
+        if (e != 0 && e != 8 && e != 16 && e != 32)
+            return fail(ctx, STNTT_EINVAL, "set_plan: elems must be 0, 8, 16 or 32");
         if (c & (c - 1))
             return fail(ctx, STNTT_EINVAL, "set_plan: cols must be 0 or a power of two");
         s.logs.push_back(lg);

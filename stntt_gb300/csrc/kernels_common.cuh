@@ -108,6 +108,28 @@ cudaError_t launch_tile_l(const PassDesc &d, const TileArgs<F> &a, uint64_t bloc
     return launch_tile_lm<F, LOGL, 1>(d, a, blocks, s);
 }
 
+// Eight elements per thread (twice the threads of a 16-element tile), tile
+// lengths 2^7..2^11: passes of small transforms, where the SMs hold too few
+// warps at 16 elements per thread.
+template <class F, int LOGL>
+cudaError_t launch_tile_l8(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks, cudaStream_t s) {
+    if (a.tw4_full && a.mode == kModeCol)
+        return launch_tile_k<F, tile_kernel_l<F, LOGL, true, 1, 8>>(d, a, blocks, s);
+    return launch_tile_k<F, tile_kernel_l<F, LOGL, false, 1, 8>>(d, a, blocks, s);
+}
+
+template <class F>
+bool launch_tile_fixed8(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks, cudaStream_t s, cudaError_t *e) {
+    switch (d.logL) {
+    case 7: *e = launch_tile_l8<F, 7>(d, a, blocks, s); return true;
+    case 8: *e = launch_tile_l8<F, 8>(d, a, blocks, s); return true;
+    case 9: *e = launch_tile_l8<F, 9>(d, a, blocks, s); return true;
+    case 10: *e = launch_tile_l8<F, 10>(d, a, blocks, s); return true;
+    case 11: *e = launch_tile_l8<F, 11>(d, a, blocks, s); return true;
+    default: return false;
+    }
+}
+
 template <class F>
 bool launch_tile_fixed(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks, cudaStream_t s, cudaError_t *e) {
     switch (d.logL) {
@@ -260,6 +282,11 @@ cudaError_t launch_tile_t(const PassDesc &d, uint32_t p, const void *tables, con
     cudaError_t e;
     if (d.E == 16 && launch_tile_fixed<F>(d, a, blocks, s, &e))
         return e;
+    if (d.E == 8 && (1u << d.logL) > 8) {  // the generic build's 8-element tiles hold one step only
+        if (launch_tile_fixed8<F>(d, a, blocks, s, &e))
+            return e;
+        return cudaErrorNotSupported;
+    }
     switch (d.E) {
     case 2: return launch_tile_e<F, 2, 1>(d, a, blocks, s);
     case 4: return launch_tile_e<F, 4, 2>(d, a, blocks, s);
@@ -419,6 +446,14 @@ cudaError_t preload_fixed_t(std::integer_sequence<int, LOGL...>) {
     return e;
 }
 
+template <class F, int... LOGL>
+cudaError_t preload_fixed8_t(std::integer_sequence<int, LOGL...>) {
+    cudaError_t e = cudaSuccess;
+    ((e = (e == cudaSuccess ? tile_attr<F, tile_kernel_l<F, LOGL + 7, false, 1, 8>>() : e)), ...);
+    ((e = (e == cudaSuccess ? tile_attr<F, tile_kernel_l<F, LOGL + 7, true, 1, 8>>() : e)), ...);
+    return e;
+}
+
 template <class F>
 cudaError_t preload_tiles_t() {
     const cudaError_t list[] = {
@@ -432,6 +467,7 @@ cudaError_t preload_tiles_t() {
         tile_attr<F, tile_kernel<F, 16, 0, true>>(), tile_attr<F, tile_kernel<F, 16, 1, true>>(),
         tile_attr<F, tile_kernel<F, 16, 2, true>>(), tile_attr<F, tile_kernel<F, 16, 3, true>>(),
         preload_fixed_t<F>(std::make_integer_sequence<int, 10>{}),
+        preload_fixed8_t<F>(std::make_integer_sequence<int, 5>{}),
     };
     for (cudaError_t e : list)
         if (e != cudaSuccess)

@@ -403,16 +403,20 @@ __device__ __forceinline__ void tile_step_l(const TileArgs<F> &a, const F &f, ty
         __syncthreads();
 }
 
-// Steps S.. of a 2^LOGL tile: one leading radix-2^(LOGL mod 4) step when LOGL
-// is not a multiple of 4, then radix-16 steps.
+// Steps S.. of a 2^LOGL tile with E elements per thread: one leading
+// radix-2^(LOGL mod log2 E) step when needed, then radix-E steps (E = 16, or
+// 8 for twice the threads on small transforms). The padding identity above
+// holds for both (checked exhaustively for every L up to 2^13).
 template <class F, int E, int LOGL, int S, class IO>
 __device__ __forceinline__ void tile_steps_l(const TileArgs<F> &a, const F &f, typename F::T (&x)[E],
                                              typename F::T *col_sm, uint32_t u, const IO &io) {
-    constexpr int TAIL = LOGL & 3;
-    constexpr int NS = (LOGL >> 2) + (TAIL > 0 ? 1 : 0);
+    static_assert(E == 8 || E == 16, "radix-8 or radix-16 steps");
+    constexpr int LE = E == 8 ? 3 : 4;  // log2 of the radix of the full steps
+    constexpr int TAIL = LOGL % LE;
+    constexpr int NS = LOGL / LE + (TAIL > 0 ? 1 : 0);
     if constexpr (S < NS) {
-        constexpr int LOGR = (S == 0 && TAIL > 0) ? TAIL : 4;
-        constexpr int LOGP = S == 0 ? 0 : (TAIL > 0 ? TAIL + 4 * (S - 1) : 4 * S);
+        constexpr int LOGR = (S == 0 && TAIL > 0) ? TAIL : LE;
+        constexpr int LOGP = S == 0 ? 0 : (TAIL > 0 ? TAIL + LE * (S - 1) : LE * S);
         tile_step_l<F, E, LOGL, LOGR, LOGP, S == 0, S == NS - 1, IO>(a, f, x, col_sm, u, io);
         tile_steps_l<F, E, LOGL, S + 1, IO>(a, f, x, col_sm, u, io);
     }
@@ -420,25 +424,26 @@ __device__ __forceinline__ void tile_steps_l(const TileArgs<F> &a, const F &f, t
 
 // One CTA's worth of work with the tile length compiled in (the counterpart
 // of tile_run for 16 elements per thread).
-template <class F, int LOGL, bool FULL4 = false>
+template <class F, int LOGL, bool FULL4 = false, int E = 16>
 __device__ __forceinline__ void tile_run_l(const TileArgs<F> &a, uint64_t blk, typename F::T *sm) {
-    static_assert(LOGL >= 4, "16 elements per thread need L >= 16");
+    static_assert(LOGL >= (E == 8 ? 3 : 4), "a tile holds at least one thread's elements");
     using T = typename F::T;
     F f;
     f.p = a.p;
     uint32_t c, u;
-    const Geo<T> g = tile_geo<F, 16>(a, blk, c, u);
-    T x[16];
-    tile_steps_l<F, 16, LOGL, 0, GlobalIO<F, FULL4>>(a, f, x, sm + c * a.cs, u, GlobalIO<F, FULL4>{g});
+    const Geo<T> g = tile_geo<F, E>(a, blk, c, u);
+    T x[E];
+    tile_steps_l<F, E, LOGL, 0, GlobalIO<F, FULL4>>(a, f, x, sm + c * a.cs, u, GlobalIO<F, FULL4>{g});
 }
 
 // MINB > 1: a build for CTAs of at most 256 threads with MINB of them resident
-// per SM (registers capped at 65536 / (256 MINB) per thread).
-template <class F, int LOGL, bool FULL4 = false, int MINB = 1>
+// per SM (registers capped at 65536 / (256 MINB) per thread). E: elements per
+// thread (16, or 8 for twice the threads on small transforms).
+template <class F, int LOGL, bool FULL4 = false, int MINB = 1, int E = 16>
 __global__ void __launch_bounds__(MINB > 1 ? 256 : 1024, MINB) tile_kernel_l(const TileArgs<F> a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     pdl_enter();
-    tile_run_l<F, LOGL, FULL4>(a, blockIdx.x, reinterpret_cast<typename F::T *>(smem_raw));
+    tile_run_l<F, LOGL, FULL4, E>(a, blockIdx.x, reinterpret_cast<typename F::T *>(smem_raw));
 }
 
 }  // namespace stntt

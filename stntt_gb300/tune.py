@@ -46,8 +46,9 @@ def splits(log_n: int, max_pass: int = 13) -> list[list[int]]:
 
 
 def candidates(field: int, log_n: int, full: bool = False) -> Iterable[tuple[list[int], list[int], list[int]]]:
-    """Plan shapes to try: every columns-per-CTA choice; without `full`, only the
-    three most even two-pass splits and the most even three-pass split."""
+    """Plan shapes to try: every columns-per-CTA choice, 16 or 32 elements per
+    thread (and 8 where every pass is 2^7..2^11 points); without `full`, only
+    the three most even two-pass splits and the most even three-pass split."""
     sp = splits(log_n)
     if not full:
         two = sorted([s for s in sp if len(s) <= 2], key=lambda s: max(s) - min(s))[:3]
@@ -55,7 +56,10 @@ def candidates(field: int, log_n: int, full: bool = False) -> Iterable[tuple[lis
         sp = two + three
     for logs in sp:
         L_min = 1 << min(logs)
-        for e in [e for e in (16, 32) if e <= L_min] or [0]:
+        es = [e for e in (16, 32) if e <= L_min]
+        if all(7 <= lg <= 11 for lg in logs) and len(logs) > 1:
+            es = [8] + es  # twice the threads per tile: for transforms too small to fill the SMs
+        for e in es or [0]:
             per_pass = []
             for lg in logs:
                 L = 1 << lg

@@ -532,3 +532,48 @@ def test_call_info_reports_launches(ctx):
     assert n == len(logs) == 2 and sum(logs) == 17
     n, logs = ctx.call_info(st.FIELD_GL64, 24, 1)
     assert n == len(logs) and sum(logs) == 24
+
+
+@pytest.mark.parametrize("field,lg,logs,cols", [
+    ("gl64", 14, [7, 7], [4, 8]), ("gl64", 18, [9, 9], [2, 4]), ("gl64", 20, [10, 10], [4, 2]),
+    ("gl64", 21, [7, 7, 7], [8, 8, 2]), ("u32", 16, [8, 8], [8, 8]), ("u32", 22, [11, 11], [2, 2])])
+def test_eight_element_tiles(ctx, field, lg, logs, cols):
+    """Plans with 8 elements per thread (radix-8 steps, twice the threads per
+    tile) are bit-exact, forward, inverse and in a polynomial product whose
+    inverse falls back to a separate pointwise product."""
+    fid = st.FIELD_GL64 if field == "gl64" else st.FIELD_U32
+    try:
+        for small in (False, True):
+            ctx.set_plan(fid, lg, logs, [8] * len(logs), cols, small=small)
+        for batch in (1, 3):
+            n = batch << lg
+            if field == "gl64":
+                x = O.uniform_u64(600 + lg + batch, n)
+                d = dev64(x)
+                ctx.ntt_gl64(d, lg, batch)
+                assert np.array_equal(host64(d), O.ntt_gl64(x, batch=batch, threads=8)), (lg, batch)
+                ctx.ntt_gl64(d, lg, batch, inverse=True)
+                assert np.array_equal(host64(d), x), (lg, batch)
+            else:
+                p, root = st.params_u32(lg)
+                x = O.uniform_u32(600 + lg + batch, p, n)
+                d = dev32(x)
+                ctx.ntt_u32(d, lg, batch, p, root)
+                assert np.array_equal(host32(d), O.ntt_u32(x, root, p, batch=batch, threads=8)), (lg, batch)
+                ctx.ntt_u32(d, lg, batch, p, root, inverse=True)
+                assert np.array_equal(host32(d), x), (lg, batch)
+        if field == "gl64" and lg <= 14:
+            n = 1 << lg
+            h = n // 2
+            a = np.zeros(n, np.uint64)
+            b = np.zeros(n, np.uint64)
+            a[:h] = O.uniform_u64(610, h)
+            b[:h] = O.uniform_u64(611, h)
+            out = torch.empty(n, dtype=torch.int64, device="cuda")
+            ctx.polymul_gl64(dev64(a), dev64(b), out, lg)
+            want = O.polymul_gl64(a[:h], b[:h])
+            assert np.array_equal(host64(out)[: want.size], want)
+    finally:
+        ctx.clear_plans()
+        from stntt_gb300 import tune
+        tune.apply_cache(ctx)
