@@ -1,0 +1,70 @@
+"""Host logic of the autotuner (no GPU): the shapes it offers and how cached
+choices are named and replayed into a context."""
+
+import json
+
+import stntt_gb300 as st
+from stntt_gb300 import tune
+
+
+def test_batched_candidates():
+    assert tune.batched_candidates(12) == [[12]]
+    c13 = tune.batched_candidates(13)
+    assert [13] in c13 and [4, 9] in c13 and [9, 4] in c13
+    c18 = tune.batched_candidates(18)
+    assert all(len(s) == 2 and sum(s) == 18 and all(4 <= x <= 13 for x in s) for s in c18)
+    assert [7, 11] in c18 and [18] not in c18
+
+
+def test_plan_candidates_offer_eight_element_tiles():
+    shapes = list(tune.candidates(st.FIELD_GL64, 20))
+    assert any(logs == [10, 10] and es == [8, 8] for logs, es, _ in shapes)
+    assert any(logs == [10, 10] and es == [16, 16] for logs, es, _ in shapes)
+    # 8 elements per thread only where every pass is 2^7..2^11 points
+    assert not any(8 in es and any(lg < 7 or lg > 11 for lg in logs) for logs, es, _ in shapes)
+    shapes24 = list(tune.candidates(st.FIELD_GL64, 24))
+    assert any(logs == [8, 8, 8] and es == [8, 8, 8] for logs, es, _ in shapes24)
+    assert not any(logs == [12, 12] and 8 in es for logs, es, _ in shapes24)
+
+
+class _FakeCtx:
+    device = 0
+
+    def __init__(self):
+        self.calls = []
+
+    def set_plan(self, field, log_n, logs, elems=None, cols=None, small=False, batched=False):
+        self.calls.append((field, log_n, list(logs), small, batched))
+
+
+def test_cache_names_and_replay(tmp_path, monkeypatch):
+    key = "TEST GPU|7|13000|10.3"
+    monkeypatch.setattr(tune, "_key", lambda device: key)
+    monkeypatch.setattr(tune, "PACKAGED", tmp_path / "none.json")
+    cache = tmp_path / "plans.json"
+    ctx = _FakeCtx()
+    tune.record(ctx, st.FIELD_GL64, 18, {"logs": [7, 11], "E": [16, 16], "C": [0, 0], "us": 1.0, "batch": 128,
+                                         "batched": True}, cache)
+    tune.record(ctx, st.FIELD_U32, 20, {"logs": [10, 10], "E": [8, 8], "C": [4, 4], "us": 2.0, "batch": 1}, cache)
+    tune.record(ctx, st.FIELD_GL64, 24, {"logs": [8, 8, 8], "E": [16] * 3, "C": [16, 16, 4], "us": 3.0, "batch": 1},
+                cache)
+    names = set(json.loads(cache.read_text())[key])
+    assert names == {"gl64:18:batch", "u32:20:b1", "gl64:24"}
+    assert tune.apply_cache(ctx, cache) == 3
+    got = {(f, lg): (small, batched) for f, lg, _, small, batched in ctx.calls}
+    assert got[(st.FIELD_GL64, 18)] == (False, True)
+    assert got[(st.FIELD_U32, 20)] == (True, False)
+    assert got[(st.FIELD_GL64, 24)] == (False, False)
+
+
+def test_packaged_plans_parse():
+    plans = json.loads(tune.PACKAGED.read_text())
+    for cls, entries in plans.items():
+        assert cls.count("|") == 1
+        for name, e in entries.items():
+            parts = name.split(":")
+            assert parts[0] in ("gl64", "u32") and len(parts) in (2, 3)
+            assert sum(e["logs"]) == int(parts[1])
+            assert len(e["logs"]) == len(e["E"]) == len(e["C"])
+            if len(parts) == 3:
+                assert parts[2] in ("b1", "batch")
