@@ -14,7 +14,8 @@
 // HBM passes.
 //
 // Inside a tile: radix-16 Stockham DIT steps (one leading radix-2/4/8 step
-// when log2 L is not a multiple of 4). A step reads R values per item into
+// when log2 L is not a multiple of 4), or radix-8 steps for the builds with 8
+// elements per thread (tile_steps_l). A step reads R values per item into
 // registers, applies w_(R p)^(r k), runs an R-point DFT as a radix-2 network
 // in registers, and writes to shared memory in Stockham order. The first
 // step reads HBM directly and the last writes HBM directly, so each element
