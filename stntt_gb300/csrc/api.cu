@@ -576,8 +576,11 @@ bool cluster_shape(const Plan &pl, uint32_t log_k, ClusterShape &cs) {
     if (pl.passes.size() != 2 || (pl.field != kFieldGL && pl.p >= (1u << 30)))
         return false;
     const PassDesc &p1 = pl.passes[0], &p2 = pl.passes[1];
-    if (p1.E != 16 || p2.E != 16 || p1.mode != kModeCol || p2.mode != kModeRow || p1.full_off == ~0ull)
+    if ((p1.E != 16 && p1.E != 8) || p2.E != p1.E || p1.mode != kModeCol || p2.mode != kModeRow ||
+        p1.full_off == ~0ull)
         return false;
+    if (p1.E == 8 && (p1.logL + p2.logL < 16 || p1.logL < 7 || p2.logL < 7))
+        return false;  // the 8-element cluster builds: 2^16- and 2^17-point splits
     // Up to 32 KiB per CTA of the cluster (256 KiB for 8 CTAs, 512 KiB for 16):
     // beyond that the cluster's SMs are compute-bound and the two-pass launches
     // were as fast or faster (measured: 8 CTAs at 2^16 Goldilocks, 2^17 32-bit).
@@ -589,8 +592,8 @@ bool cluster_shape(const Plan &pl, uint32_t log_k, ClusterShape &cs) {
     cs.d1 = p1;
     cs.d2 = p2;
     cs.log_k = log_k;
-    shape_pass(cs.d1, pl.field, 1ull << p1.logS, 16, 1u << (L2 - log_k));  // column limit: the sub-problem's columns
-    shape_pass(cs.d2, pl.field, 1ull << 20, 16, 1u << (L1 - log_k));
+    shape_pass(cs.d1, pl.field, 1ull << p1.logS, p1.E, 1u << (L2 - log_k));  // column limit: the sub-problem's columns
+    shape_pass(cs.d2, pl.field, 1ull << 20, p1.E, 1u << (L1 - log_k));
     if (cs.d1.logC != L2 - log_k || cs.d2.logC != L1 - log_k || cs.d1.threads != cs.d2.threads)
         return false;
     const size_t esz = pl.field == kFieldGL ? 8 : 4;

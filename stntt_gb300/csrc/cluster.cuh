@@ -55,8 +55,9 @@ struct ClusterGatherIO {
 
 // a1 / a2: the plan's two passes, reshaped to n2/K columns and n1/K rows per
 // CTA. xoff: element offset of the exchange buffer in shared memory; xs: its
-// column stride. Grid: K CTAs per transform, cluster dimension K.
-template <class F, int LOG1, int LOG2, bool FULL4>
+// column stride. Grid: K CTAs per transform, cluster dimension K. E: elements
+// per thread of both passes (16, or 8 for twice the threads per CTA).
+template <class F, int LOG1, int LOG2, bool FULL4, int E = 16>
 __global__ void __launch_bounds__(1024) cluster_kernel(const TileArgs<F> a1, const TileArgs<F> a2, uint32_t xoff,
                                                        uint32_t xs) {
     using T = typename F::T;
@@ -68,20 +69,20 @@ __global__ void __launch_bounds__(1024) cluster_kernel(const TileArgs<F> a1, con
     const uint64_t blk = blockIdx.x;  // tile index over the batch: transform blk / K, cluster rank blk mod K
     F f;
     f.p = a1.p;
-    T x[16];
+    T x[E];
     {
         uint32_t c, u;
-        const Geo<T> g = tile_geo<F, 16>(a1, blk, c, u);
-        tile_steps_l<F, 16, LOG1, 0, ExchangeStoreIO<F, FULL4>>(a1, f, x, work + c * a1.cs, u,
-                                                                ExchangeStoreIO<F, FULL4>{g, xbuf + c * xs});
+        const Geo<T> g = tile_geo<F, E>(a1, blk, c, u);
+        tile_steps_l<F, E, LOG1, 0, ExchangeStoreIO<F, FULL4>>(a1, f, x, work + c * a1.cs, u,
+                                                               ExchangeStoreIO<F, FULL4>{g, xbuf + c * xs});
     }
     cl.sync();
     {
         uint32_t c, u;
-        const Geo<T> g = tile_geo<F, 16>(a2, blk, c, u);
+        const Geo<T> g = tile_geo<F, E>(a2, blk, c, u);
         const uint32_t row = (uint32_t)(cl.block_rank() << a2.logC) + c;
-        tile_steps_l<F, 16, LOG2, 0, ClusterGatherIO<F>>(a2, f, x, work + c * a2.cs, u,
-                                                         ClusterGatherIO<F>{g, xbuf, row, a1.logC, xs});
+        tile_steps_l<F, E, LOG2, 0, ClusterGatherIO<F>>(a2, f, x, work + c * a2.cs, u,
+                                                        ClusterGatherIO<F>{g, xbuf, row, a1.logC, xs});
     }
     cl.sync();
 }

@@ -169,11 +169,11 @@ cudaError_t cluster_attr() {
     return cudaSuccess;
 }
 
-template <class F, int LOG1, int LOG2>
+template <class F, int LOG1, int LOG2, int E = 16>
 cudaError_t launch_cluster_k(const TileArgs<F> &a1, const TileArgs<F> &a2, uint32_t xoff, uint32_t xs,
                              uint64_t blocks, uint32_t threads, size_t smem, uint32_t log_k, cudaStream_t s) {
-    auto kern = cluster_kernel<F, LOG1, LOG2, true>;
-    cudaError_t e = cluster_attr<F, cluster_kernel<F, LOG1, LOG2, true>>();
+    auto kern = cluster_kernel<F, LOG1, LOG2, true, E>;
+    cudaError_t e = cluster_attr<F, cluster_kernel<F, LOG1, LOG2, true, E>>();
     if (e != cudaSuccess)
         return e;
     if (smem > 200 * 1024 || blocks > 0x7fffffffull)
@@ -326,6 +326,16 @@ cudaError_t launch_cluster_t(const PassDesc &d1, const PassDesc &d2, uint32_t p,
         return cudaErrorNotSupported;
     const uint64_t blocks = batch << log_k;
     const uint32_t t = d1.threads;
+    if (d1.E == 8) {  // 8 elements per thread: the 2^16- and 2^17-point splits
+        switch (d1.logL * 16 + d2.logL) {
+        case 8 * 16 + 8: return launch_cluster_k<F, 8, 8, 8>(a1, a2, xoff, xs, blocks, t, smem, log_k, s);
+        case 7 * 16 + 9: return launch_cluster_k<F, 7, 9, 8>(a1, a2, xoff, xs, blocks, t, smem, log_k, s);
+        case 9 * 16 + 7: return launch_cluster_k<F, 9, 7, 8>(a1, a2, xoff, xs, blocks, t, smem, log_k, s);
+        case 8 * 16 + 9: return launch_cluster_k<F, 8, 9, 8>(a1, a2, xoff, xs, blocks, t, smem, log_k, s);
+        case 9 * 16 + 8: return launch_cluster_k<F, 9, 8, 8>(a1, a2, xoff, xs, blocks, t, smem, log_k, s);
+        default: return cudaErrorNotSupported;
+        }
+    }
     switch (d1.logL * 16 + d2.logL) {
     case 7 * 16 + 7: return launch_cluster_k<F, 7, 7>(a1, a2, xoff, xs, blocks, t, smem, log_k, s);
     case 7 * 16 + 8: return launch_cluster_k<F, 7, 8>(a1, a2, xoff, xs, blocks, t, smem, log_k, s);
@@ -372,6 +382,9 @@ cudaError_t preload_clusters_t() {
         cluster_attr<F, cluster_kernel<F, 8, 7, true>>(), cluster_attr<F, cluster_kernel<F, 7, 9, true>>(),
         cluster_attr<F, cluster_kernel<F, 8, 8, true>>(), cluster_attr<F, cluster_kernel<F, 9, 7, true>>(),
         cluster_attr<F, cluster_kernel<F, 8, 9, true>>(), cluster_attr<F, cluster_kernel<F, 9, 8, true>>(),
+        cluster_attr<F, cluster_kernel<F, 8, 8, true, 8>>(), cluster_attr<F, cluster_kernel<F, 7, 9, true, 8>>(),
+        cluster_attr<F, cluster_kernel<F, 9, 7, true, 8>>(), cluster_attr<F, cluster_kernel<F, 8, 9, true, 8>>(),
+        cluster_attr<F, cluster_kernel<F, 9, 8, true, 8>>(),
     };
     for (cudaError_t e : list)
         if (e != cudaSuccess)

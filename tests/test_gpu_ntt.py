@@ -577,3 +577,36 @@ def test_eight_element_tiles(ctx, field, lg, logs, cols):
         ctx.clear_plans()
         from stntt_gb300 import tune
         tune.apply_cache(ctx)
+
+
+@pytest.mark.parametrize("field,lg,logs", [("u32", 16, [8, 8]), ("u32", 17, [8, 9]), ("gl64", 16, [8, 8]),
+                                           ("gl64", 16, [9, 7])])
+def test_cluster_path_eight_elements(ctx, field, lg, logs):
+    """Small-call plans with 8 elements per thread run the cluster path with
+    twice the threads per CTA where its shape allows it; bit-exact either way."""
+    fid = st.FIELD_GL64 if field == "gl64" else st.FIELD_U32
+    try:
+        ctx.set_plan(fid, lg, logs, [8, 8], small=True)
+        p, root = (0, 0) if field == "gl64" else st.params_u32(lg)
+        launches, _ = ctx.call_info(fid, lg, 1, p, root)
+        assert launches in (1, 2)
+        for batch in (1, 3):
+            n = batch << lg
+            if field == "gl64":
+                x = O.uniform_u64(700 + lg + batch, n)
+                d = dev64(x)
+                ctx.ntt_gl64(d, lg, batch)
+                assert np.array_equal(host64(d), O.ntt_gl64(x, batch=batch, threads=8)), (lg, batch)
+                ctx.ntt_gl64(d, lg, batch, inverse=True)
+                assert np.array_equal(host64(d), x), (lg, batch)
+            else:
+                x = O.uniform_u32(700 + lg + batch, p, n)
+                d = dev32(x)
+                ctx.ntt_u32(d, lg, batch, p, root)
+                assert np.array_equal(host32(d), O.ntt_u32(x, root, p, batch=batch, threads=8)), (lg, batch)
+                ctx.ntt_u32(d, lg, batch, p, root, inverse=True)
+                assert np.array_equal(host32(d), x), (lg, batch)
+    finally:
+        ctx.clear_plans()
+        from stntt_gb300 import tune
+        tune.apply_cache(ctx)
