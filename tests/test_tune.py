@@ -68,3 +68,12 @@ def test_packaged_plans_parse():
             assert len(e["logs"]) == len(e["E"]) == len(e["C"])
             if len(parts) == 3:
                 assert parts[2] in ("b1", "batch")
+            # what the library accepts (a rejected entry would make every Context fail)
+            assert 1 <= len(e["logs"]) <= 3 and all(1 <= lg <= 13 for lg in e["logs"])
+            assert all(x in (0, 8, 16, 32) for x in e["E"])
+            if 8 in e["E"]:
+                assert all(7 <= lg <= 11 for lg in e["logs"]), name
+            if name.endswith(":batch"):
+                assert len(e["logs"]) <= 2 and all(lg >= 4 for lg in e["logs"]), name
+                if len(e["logs"]) == 2:
+                    assert int(parts[1]) >= 13, name
