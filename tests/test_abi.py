@@ -54,3 +54,23 @@ def test_no_cpu_fallback_without_gpu(stntt_lib):
     assert stntt_lib.stntt_init(C.byref(h), 0) != 0
     with pytest.raises(st.StnttError):
         st.Context(0)
+
+
+def test_header_compiles_as_c_and_links(stntt_lib, tmp_path):
+    """include/stntt.h is plain C: a C11 host (tests/cpp/c_abi_check.c, the
+    calls of a single transform, an uneven batch, device-side parameters, the
+    TMA switch and the allocation-free entry point) compiles warning-free with
+    -pedantic and links against libstntt."""
+    import shutil
+    from pathlib import Path
+
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not available")
+    root = Path(__file__).resolve().parents[1]
+    exe = tmp_path / "c_abi_check"
+    so_dir = st.SO_PATH.parent
+    r = subprocess.run(["gcc", "-std=c11", "-Wall", "-Wextra", "-pedantic", "-Werror", f"-I{root / 'include'}",
+                        str(root / "tests" / "cpp" / "c_abi_check.c"), "-o", str(exe), f"-L{so_dir}", "-lstntt",
+                        f"-Wl,-rpath,{so_dir}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert exe.exists()
