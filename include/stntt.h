@@ -66,6 +66,14 @@ const char *stntt_status_string(int status);
 int stntt_version(void);
 /* Bytes of device memory the context currently holds (tables + workspaces). */
 int stntt_mem_usage(const stntt_ctx *ctx, size_t *bytes);
+/* Free the scratch the context keeps for `stream` (the buffer between HBM
+ * passes, one per stream a multi-pass transform ran on), after waiting for the
+ * stream's work. A caller that makes a stream per request releases it before
+ * destroying the stream; the context also keeps at most 16 such buffers and
+ * frees the least recently used one (after waiting for its stream) when a
+ * 17th stream appears. No counterpart in the reference, which allocates and
+ * frees a double buffer on every autoNtt call (src/cuda/ntt/ntt_kernel.cuh:157-160). */
+int stntt_release_stream(stntt_ctx *ctx, stntt_stream stream);
 
 /* ---- parameters ------------------------------------------------------------- */
 /* findParams(size, min_mod) -> (root, mod): src/ntt/ntt_util.cpp:10-14
@@ -159,6 +167,13 @@ int stntt_ntt_u32_steps(stntt_ctx *ctx, uint32_t *d_data, uint32_t log_n, uint32
 int stntt_ntt_stockham_host(stntt_ctx *ctx, int32_t *vec, int32_t size, int32_t root, int32_t mod,
                             int32_t batches, int32_t nsteps, uint32_t flags);
 int stntt_ntt_gl64_host(stntt_ctx *ctx, uint64_t *vec, uint32_t log_n, uint32_t batch, int dir);
+/* Device time, in milliseconds, of the last host-buffer call on this context
+ * (stntt_ntt_stockham_host or stntt_ntt_gl64_host): CUDA events recorded
+ * after the copy in and before the copy out, around the transform's kernels.
+ * The value cuda::ntt::autoNtt<n> returns as its kernel time
+ * (src/cuda/ntt/ntt_kernel.cuh:167,187-191; stored as gpuTime by
+ * src/bench.cu:48-50). */
+int stntt_last_kernel_ms(stntt_ctx *ctx, float *ms);
 
 /* ---- uneven batches ----------------------------------------------------------- */
 typedef struct stntt_job {
@@ -287,8 +302,11 @@ int stntt_server_destroy(stntt_server *sv);
  * fixed array inside the library (8 MiB + 256 KiB per GPU, kept until exit),
  * so batch * 2^log_n must be <= 2^20 (else STNTT_EUNSUPPORTED). All calls
  * share that array: calls that overlap on the GPU race, so order them on one
- * stream. The first call on a device looks up the array's address; make it
- * before capturing a stream into a CUDA graph. d_in may equal d_out. */
+ * stream. CUDA loads the library's device code on first use, so the first
+ * call on a device may reserve the array and load the kernels: make that
+ * first call (a warm-up) before a pool takes the rest of HBM and before
+ * capturing a stream into a CUDA graph; if the array cannot be placed the
+ * call returns STNTT_ENOMEM. d_in may equal d_out. */
 int stntt_ntt_gl64_noalloc(const uint64_t *d_in, uint64_t *d_out, uint32_t log_n, uint32_t batch, int dir,
                            stntt_stream stream);
 

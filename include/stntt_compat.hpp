@@ -98,15 +98,20 @@ struct NttArgs {
     }
 };
 
-// In place on args.vec (host memory), like the reference. Returns 0: time
-// kernels with CUDA events around stntt_ntt_u32 on device data instead.
+// In place on args.vec (host memory), like the reference. Returns the device
+// time of the transform in milliseconds, measured with CUDA events recorded
+// after the copy in and before the copy out, as the reference's autoNtt does
+// (ntt_kernel.cuh:167,187-191).
 template <size_t n>
 float autoNtt(NttArgs args) {
     if (args.n != n)
         throw std::invalid_argument("autoNtt<n>: args.n differs from n");
     ::nttStockham(args.vec, static_cast<int>(n), static_cast<int>(args.root), static_cast<int>(args.mod),
                   static_cast<int>(args.batches));
-    return 0.f;
+    stntt_ctx *ctx = stntt_compat::default_ctx();
+    float ms = 0.f;
+    stntt_compat::check(stntt_last_kernel_ms(ctx, &ms), ctx);
+    return ms;
 }
 
 }  // namespace cuda::ntt

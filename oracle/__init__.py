@@ -31,11 +31,33 @@ _u64p = np.ctypeslib.ndpointer(np.uint64, flags="C_CONTIGUOUS")
 _i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
 
 
+def ref_sources() -> Path | None:
+    """The reference sources the baselines compile from: $STNTT_REF_DIR, else
+    the copy staged in baseline/_ref (``make -C oracle ref-stage REF=...``)."""
+    for cand in (os.environ.get("STNTT_REF_DIR"), str(HERE.parent / "baseline" / "_ref")):
+        if cand and (Path(cand) / "src" / "ntt" / "ntt_cpu.cpp").exists():
+            return Path(cand)
+    return None
+
+
 def build(ref: bool = False) -> None:
-    """Compile the oracle library (and, with ``ref``, the reference CPU code)."""
+    """Compile the oracle library (and, with ``ref``, the reference CPU code
+    and the reference GPU benchmark driver)."""
     subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
     if ref:
-        subprocess.run(["make", "-s", "-C", str(HERE), "ref"], check=True)
+        src = ref_sources()
+        env = dict(os.environ, REF=str(src)) if src else None
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref"], check=True, env=env)
+        # the reference's CUDA code (nvcc, sm_100): a missing toolkit only costs that baseline
+        r = subprocess.run(["make", "-s", "-C", str(HERE), "ref-gpu"], env=env, capture_output=True, text=True)
+        if r.returncode != 0:
+            print(f"reference GPU benchmark not built: {r.stderr.strip()[-300:]}")
+
+
+def ref_gpu_bench() -> Path | None:
+    """The reference CUDA NTT benchmark driver built by ``make ref-gpu``."""
+    exe = HERE / "_ref" / platform.machine() / "ref_gpu_bench"
+    return exe if exe.exists() else None
 
 
 def _bind(lib, name, res, args):
@@ -79,6 +101,8 @@ def lib():
         _bind(L, "orc_fnv1a64", u64, [C.c_void_p, sz])
         _bind(L, "orc_dft_point_u32", u32, [_u32p, u64, u32, u32, u64])
         _bind(L, "orc_dft_point_gl64", u64, [_u64p, u64, u64, u64])
+        _bind(L, "orc_cyclic_conv_u32", C.c_int, [_u32p, _u32p, u32, u32, u32])
+        _bind(L, "orc_cyclic_conv_gl64", C.c_int, [_u64p, _u64p, u32])
         _lib = L
     return _lib
 
@@ -208,6 +232,23 @@ def polymul_gl64(a, b) -> np.ndarray:
     out = np.empty(a.size + b.size - 1, np.uint64)
     lib().orc_polymul_gl64(a, a.size, b, b.size, out)
     return out
+
+
+def cyclic_conv_u32(a, b, root: int, mod: int) -> np.ndarray:
+    """Length-n cyclic convolution through the transform (pwcNtt semantics)."""
+    x = np.ascontiguousarray(a, dtype=np.uint32).copy()
+    y = np.ascontiguousarray(b, dtype=np.uint32).copy()
+    if lib().orc_cyclic_conv_u32(x, y, x.size, root, mod):
+        raise RuntimeError("orc_cyclic_conv_u32 failed")
+    return x
+
+
+def cyclic_conv_gl64(a, b) -> np.ndarray:
+    x = np.ascontiguousarray(a, dtype=np.uint64).copy()
+    y = np.ascontiguousarray(b, dtype=np.uint64).copy()
+    if lib().orc_cyclic_conv_gl64(x, y, x.size):
+        raise RuntimeError("orc_cyclic_conv_gl64 failed")
+    return x
 
 
 def ntt_ct_u32(vec, root: int, mod: int) -> np.ndarray:

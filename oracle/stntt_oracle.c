@@ -652,6 +652,38 @@ void orc_polymul_gl64(const uint64_t *a, size_t na, const uint64_t *b, size_t nb
             out[i + j] = gl_add(out[i + j], orc_gl_mul(a[i], b[j]));
 }
 
+/* Cyclic convolution of length n through the transform, the semantics of
+ * pwcNtt (ntt_cpu.cpp:167-174): forward transform of both inputs, element-wise
+ * product (elemWiseMul, ntt_util.h:29-33, with exact products here), inverse
+ * scaled by n^-1. The reference goes NO->BO->NO (nttCt / inttGs); natural
+ * order on both sides gives the same result. a is overwritten with the
+ * result, b with its transform. */
+int orc_cyclic_conv_u32(uint32_t *a, uint32_t *b, uint32_t n, uint32_t root, uint32_t mod) {
+    int rc = orc_ntt_u32(a, n, root, mod, -1);
+    if (!rc)
+        rc = orc_ntt_u32(b, n, root, mod, -1);
+    if (rc)
+        return rc;
+    for (uint32_t i = 0; i < n; ++i)
+        a[i] = (uint32_t)((uint64_t)a[i] * b[i] % mod);
+    return orc_intt_u32(a, n, root, mod);
+}
+
+int orc_cyclic_conv_gl64(uint64_t *a, uint64_t *b, uint32_t n) {
+    int lg = log2_exact(n);
+    if (lg < 0)
+        return -1;
+    const uint64_t root = orc_gl_root((uint32_t)lg);
+    int rc = orc_ntt_gl64(a, n, root, -1);
+    if (!rc)
+        rc = orc_ntt_gl64(b, n, root, -1);
+    if (rc)
+        return rc;
+    for (uint32_t i = 0; i < n; ++i)
+        a[i] = orc_gl_mul(a[i], b[i]);
+    return orc_intt_gl64(a, n, root);
+}
+
 uint64_t orc_fnv1a64(const void *data, size_t nbytes) {
     const unsigned char *p = (const unsigned char *)data;
     uint64_t h = 0xcbf29ce484222325ull;

@@ -78,6 +78,12 @@ uint64_t orc_dft_point_gl64(const uint64_t *in, uint64_t n, uint64_t root, uint6
 void orc_polymul_u32(const uint32_t *a, size_t na, const uint32_t *b, size_t nb, uint32_t mod, uint32_t *out);
 void orc_polymul_gl64(const uint64_t *a, size_t na, const uint64_t *b, size_t nb, uint64_t *out);
 
+/* Cyclic convolution of length n via forward, element-wise product and
+ * inverse (pwcNtt semantics, ntt_cpu.cpp:167-174). a <- a (*) b; b is
+ * overwritten with its transform. */
+int orc_cyclic_conv_u32(uint32_t *a, uint32_t *b, uint32_t n, uint32_t root, uint32_t mod);
+int orc_cyclic_conv_gl64(uint64_t *a, uint64_t *b, uint32_t n);
+
 /* ---- misc ------------------------------------------------------------------ */
 uint64_t orc_fnv1a64(const void *data, size_t nbytes);
 

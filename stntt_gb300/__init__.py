@@ -89,6 +89,8 @@ _SIGS = {
     "stntt_destroy": (_int, [_vp]),
     "stntt_last_error": (C.c_char_p, [_vp]),
     "stntt_mem_usage": (_int, [_vp, C.POINTER(_sz)]),
+    "stntt_release_stream": (_int, [_vp, _vp]),
+    "stntt_last_kernel_ms": (_int, [_vp, C.POINTER(C.c_float)]),
     "stntt_find_params": (_int, [_u64, _u64, C.POINTER(_u64), C.POINTER(_u64)]),
     "stntt_find_params_device": (_int, [_u64, _u64, _vp, _vp]),
     "stntt_params_u32": (_int, [_u32, C.POINTER(_u32), C.POINTER(_u32)]),
@@ -282,6 +284,16 @@ class Context:
         b = _sz()
         _check(lib().stntt_mem_usage(self._h, C.byref(b)), self._h)
         return b.value
+
+    def release_stream(self, stream) -> None:
+        """Free the scratch kept for `stream` (stntt_release_stream)."""
+        _check(lib().stntt_release_stream(self._h, _stream(stream)), self._h)
+
+    def last_kernel_ms(self) -> float:
+        """Device time of the last host-buffer call (stntt_last_kernel_ms)."""
+        ms = C.c_float()
+        _check(lib().stntt_last_kernel_ms(self._h, C.byref(ms)), self._h)
+        return ms.value
 
     def prepare(self, field: int, log_n: int, p: int = 0, root: int = 0, inverse: bool = False) -> None:
         _check(lib().stntt_prepare(self._h, field, log_n, p, root, INVERSE if inverse else FORWARD), self._h)

@@ -222,6 +222,16 @@ struct DevBuf {
     size_t bytes = 0;
 };
 
+// A stream's scratch buffer and when it was last handed out.
+struct StreamBuf {
+    DevBuf buf;
+    uint64_t last_use = 0;
+};
+
+// Streams whose scratch a context keeps at once (the serving loop uses one
+// per slot, up to 32); beyond this the least recently used buffer is freed.
+constexpr size_t kMaxStreamWorkspaces = 64;
+
 // A plan shape chosen by the caller (the autotuner) instead of the default.
 struct PlanSpec {
     std::vector<uint32_t> logs, elems, cols;
@@ -235,13 +245,18 @@ struct stntt_ctx {
     std::mutex mu;
     std::map<PlanKey, std::unique_ptr<Plan>> plans;
     std::map<std::tuple<uint32_t, uint32_t, uint32_t, int>, DevBuf> stage_tables;  // (log_n, p, root, wrap)
-    std::map<cudaStream_t, DevBuf> workspaces;
+    std::map<cudaStream_t, StreamBuf> workspaces;
+    uint64_t ws_clock = 0;
     std::map<std::tuple<int, uint32_t, int>, PlanSpec> specs;  // (field, log_n, kind) -> override
     cudaStream_t setup = nullptr;
     // host-buffer calls: one at a time, on their own stream and staging buffer
     std::mutex host_mu;
     cudaStream_t host_stream = nullptr;
     DevBuf host_stage;
+    // CUDA events around the device work of the last host-buffer call, and
+    // its duration (the reference's autoNtt returns this "kernel time")
+    cudaEvent_t host_ev0 = nullptr, host_ev1 = nullptr;
+    float host_kernel_ms = 0.f;
     std::string err;
     size_t mem = 0;
     uint32_t cluster_log = 3;  // log2 of the cluster size the one-launch transforms use (3 or 4)
@@ -517,32 +532,71 @@ int get_plan(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t p, uint64_t roo
     return STNTT_OK;
 }
 
-// Per-stream scratch of at least `bytes`.
+// Per-stream scratch of at least `bytes`. A buffer that must grow, and the
+// least recently used one when a stream beyond kMaxStreamWorkspaces appears,
+// is taken out of the map under the lock and waited for and freed outside it,
+// so other threads on the context do not stall behind that wait.
 int get_workspace(stntt_ctx *ctx, cudaStream_t s, size_t bytes, void **ptr) {
-    std::lock_guard<std::mutex> g(ctx->mu);
-    DevBuf &b = ctx->workspaces[s];
-    if (b.bytes < bytes) {
-        if (b.ptr) {
-            cudaError_t e = cudaStreamSynchronize(s);
-            if (e != cudaSuccess) {
-                ctx->err = std::string("workspace resize sync: ") + cudaGetErrorString(e);
-                return STNTT_ECUDA;
-            }
-            cudaFree(b.ptr);
-            ctx->mem -= b.bytes;
-            b.ptr = nullptr;
-            b.bytes = 0;
+    StreamBuf old, victim;
+    cudaStream_t victim_s = nullptr;
+    {
+        std::lock_guard<std::mutex> g(ctx->mu);
+        auto it = ctx->workspaces.find(s);
+        if (it != ctx->workspaces.end() && it->second.buf.bytes >= bytes) {
+            it->second.last_use = ++ctx->ws_clock;
+            *ptr = it->second.buf.ptr;
+            return STNTT_OK;
         }
-        cudaError_t e = cudaMalloc(&b.ptr, bytes);
-        if (e != cudaSuccess) {
-            b.ptr = nullptr;
-            ctx->err = std::string("cudaMalloc(workspace): ") + cudaGetErrorString(e);
-            return e == cudaErrorMemoryAllocation ? STNTT_ENOMEM : STNTT_ECUDA;
+        if (it != ctx->workspaces.end()) {
+            old = it->second;
+            ctx->workspaces.erase(it);
+        } else if (ctx->workspaces.size() >= kMaxStreamWorkspaces) {
+            auto lru = ctx->workspaces.begin();
+            for (auto j = ctx->workspaces.begin(); j != ctx->workspaces.end(); ++j)
+                if (j->second.last_use < lru->second.last_use)
+                    lru = j;
+            victim = lru->second;
+            victim_s = lru->first;
+            ctx->workspaces.erase(lru);
         }
-        b.bytes = bytes;
-        ctx->mem += bytes;
+        ctx->mem -= old.buf.bytes + victim.buf.bytes;
     }
-    *ptr = b.ptr;
+    if (old.buf.ptr) {
+        const cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess)
+            return cuda_fail(ctx, e, "workspace resize: waiting for the stream");
+        cudaFree(old.buf.ptr);
+    }
+    if (victim.buf.ptr) {
+        if (cudaStreamSynchronize(victim_s) != cudaSuccess) {  // e.g. a stream destroyed without release
+            cudaGetLastError();
+            cudaDeviceSynchronize();
+        }
+        cudaFree(victim.buf.ptr);
+    }
+    StreamBuf nb;
+    const cudaError_t e = cudaMalloc(&nb.buf.ptr, bytes);
+    if (e != cudaSuccess)
+        return fail(ctx, e == cudaErrorMemoryAllocation ? STNTT_ENOMEM : STNTT_ECUDA,
+                    std::string("cudaMalloc(workspace): ") + cudaGetErrorString(e));
+    nb.buf.bytes = bytes;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    nb.last_use = ++ctx->ws_clock;
+    auto ins = ctx->workspaces.emplace(s, nb);
+    if (!ins.second) {  // another thread on the same stream stored one meanwhile
+        if (ins.first->second.buf.bytes >= bytes) {
+            cudaFree(nb.buf.ptr);
+            *ptr = ins.first->second.buf.ptr;
+            return STNTT_OK;
+        }
+        // both were ordered on this stream: the smaller one is idle once the stream is
+        cudaStreamSynchronize(s);
+        cudaFree(ins.first->second.buf.ptr);
+        ctx->mem -= ins.first->second.buf.bytes;
+        ins.first->second = nb;
+    }
+    ctx->mem += bytes;
+    *ptr = nb.buf.ptr;
     return STNTT_OK;
 }
 
@@ -769,6 +823,25 @@ int host_stage(stntt_ctx *ctx, size_t bytes, void **ptr) {
     return STNTT_OK;
 }
 
+// The end of a host-buffer call (caller holds host_mu): stop the device-work
+// event, copy the result back, wait, and keep the device time between the two
+// events for stntt_last_kernel_ms.
+int host_finish(stntt_ctx *ctx, void *host, const void *dev, size_t bytes, cudaStream_t s) {
+    cudaError_t e = cudaEventRecord(ctx->host_ev1, s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "host copy out");
+    float ms = 0.f;
+    e = cudaEventElapsedTime(&ms, ctx->host_ev0, ctx->host_ev1);
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "cudaEventElapsedTime");
+    ctx->host_kernel_ms = ms;
+    return STNTT_OK;
+}
+
 int ctx_device(const stntt_ctx *ctx) { return ctx->device; }
 
 // Drop every cached plan (caller holds ctx->mu; the device is idle).
@@ -781,16 +854,21 @@ void drop_plans(stntt_ctx *ctx) {
     ctx->plans.clear();
 }
 
-void release_workspace(stntt_ctx *ctx, cudaStream_t s) {
-    std::lock_guard<std::mutex> g(ctx->mu);
-    auto it = ctx->workspaces.find(s);
-    if (it == ctx->workspaces.end())
-        return;
-    cudaStreamSynchronize(s);
-    if (it->second.ptr)
-        cudaFree(it->second.ptr);
-    ctx->mem -= it->second.bytes;
-    ctx->workspaces.erase(it);
+int release_workspace(stntt_ctx *ctx, cudaStream_t s) {
+    StreamBuf b;
+    {
+        std::lock_guard<std::mutex> g(ctx->mu);
+        auto it = ctx->workspaces.find(s);
+        if (it == ctx->workspaces.end())
+            return STNTT_OK;
+        b = it->second;
+        ctx->mem -= b.buf.bytes;
+        ctx->workspaces.erase(it);
+    }
+    const cudaError_t e = cudaStreamSynchronize(s);
+    if (b.buf.ptr)
+        cudaFree(b.buf.ptr);
+    return e == cudaSuccess ? STNTT_OK : cuda_fail(ctx, e, "release_stream: waiting for the stream");
 }
 
 }  // namespace sd
@@ -826,33 +904,34 @@ int stntt_init(stntt_ctx **out, int device) {
         return STNTT_ENOMEM;
     ctx->device = device;
     DeviceGuard g(device);
-    if (g.err != cudaSuccess || cudaStreamCreateWithFlags(&ctx->setup, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&ctx->host_stream, cudaStreamNonBlocking) != cudaSuccess) {
-        if (ctx->setup)
-            cudaStreamDestroy(ctx->setup);
-        delete ctx;
-        return STNTT_ECUDA;
-    }
-    if (cluster_max_size() >= 16)
-        ctx->cluster_log = kClusterLogLarge;
-    if (cudaMalloc(&ctx->d_err, sizeof(int)) != cudaSuccess || cudaMemset(ctx->d_err, 0, sizeof(int)) != cudaSuccess) {
+    // release whatever was created before a failing step
+    auto undo = [ctx](int status) {
         if (ctx->d_err)
             cudaFree(ctx->d_err);
-        cudaStreamDestroy(ctx->setup);
-        cudaStreamDestroy(ctx->host_stream);
+        if (ctx->host_ev0)
+            cudaEventDestroy(ctx->host_ev0);
+        if (ctx->host_ev1)
+            cudaEventDestroy(ctx->host_ev1);
+        if (ctx->setup)
+            cudaStreamDestroy(ctx->setup);
+        if (ctx->host_stream)
+            cudaStreamDestroy(ctx->host_stream);
         delete ctx;
-        return STNTT_ENOMEM;
-    }
+        return status;
+    };
+    if (g.err != cudaSuccess || cudaStreamCreateWithFlags(&ctx->setup, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->host_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&ctx->host_ev0) != cudaSuccess || cudaEventCreate(&ctx->host_ev1) != cudaSuccess)
+        return undo(STNTT_ECUDA);
+    if (cluster_max_size() >= 16)
+        ctx->cluster_log = kClusterLogLarge;
+    if (cudaMalloc(&ctx->d_err, sizeof(int)) != cudaSuccess || cudaMemset(ctx->d_err, 0, sizeof(int)) != cudaSuccess)
+        return undo(STNTT_ENOMEM);
     // Load every kernel now: a lazy load at first use would stall the device
     // in the middle of a caller's stream of work. This also fails early when
     // the library holds no code for this GPU.
-    if (preload_kernels() != cudaSuccess) {
-        cudaFree(ctx->d_err);
-        cudaStreamDestroy(ctx->setup);
-        cudaStreamDestroy(ctx->host_stream);
-        delete ctx;
-        return STNTT_ECUDA;
-    }
+    if (preload_kernels() != cudaSuccess)
+        return undo(STNTT_ECUDA);
     *out = ctx;
     return STNTT_OK;
 }
@@ -866,8 +945,8 @@ int stntt_destroy(stntt_ctx *ctx) {
         if (kv.second->d_tables)
             cudaFree(kv.second->d_tables);
     for (auto &kv : ctx->workspaces)
-        if (kv.second.ptr)
-            cudaFree(kv.second.ptr);
+        if (kv.second.buf.ptr)
+            cudaFree(kv.second.buf.ptr);
     for (auto &kv : ctx->stage_tables)
         if (kv.second.ptr)
             cudaFree(kv.second.ptr);
@@ -879,6 +958,10 @@ int stntt_destroy(stntt_ctx *ctx) {
         cudaStreamDestroy(ctx->setup);
     if (ctx->host_stream)
         cudaStreamDestroy(ctx->host_stream);
+    if (ctx->host_ev0)
+        cudaEventDestroy(ctx->host_ev0);
+    if (ctx->host_ev1)
+        cudaEventDestroy(ctx->host_ev1);
     delete ctx;
     return STNTT_OK;
 }
@@ -889,6 +972,21 @@ int stntt_mem_usage(const stntt_ctx *ctx, size_t *bytes) {
     if (!ctx || !bytes)
         return STNTT_EINVAL;
     *bytes = ctx->mem;
+    return STNTT_OK;
+}
+
+int stntt_release_stream(stntt_ctx *ctx, stntt_stream stream) {
+    if (!ctx)
+        return STNTT_EINVAL;
+    DeviceGuard g(ctx->device);
+    return release_workspace(ctx, (cudaStream_t)stream);
+}
+
+int stntt_last_kernel_ms(stntt_ctx *ctx, float *ms) {
+    if (!ctx || !ms)
+        return STNTT_EINVAL;
+    std::lock_guard<std::mutex> hl(ctx->host_mu);
+    *ms = ctx->host_kernel_ms;
     return STNTT_OK;
 }
 
@@ -1287,6 +1385,9 @@ int stntt_ntt_stockham_host(stntt_ctx *ctx, int32_t *vec, int32_t size, int32_t 
     cudaError_t e = cudaMemcpyAsync(d, src, count * 4, cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess)
         return cuda_fail(ctx, e, "host copy in");
+    e = cudaEventRecord(ctx->host_ev0, s);
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "cudaEventRecord");
     if (nsteps >= 0 && (uint32_t)nsteps < log_n)
         rc = stntt_ntt_u32_steps(ctx, d, log_n, (uint32_t)batches, (uint32_t)mod, (uint32_t)root, (uint32_t)nsteps,
                                  flags, s);
@@ -1296,12 +1397,7 @@ int stntt_ntt_stockham_host(stntt_ctx *ctx, int32_t *vec, int32_t size, int32_t 
         cudaStreamSynchronize(s);
         return rc;
     }
-    e = cudaMemcpyAsync(vec, d, count * 4, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess)
-        e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess)
-        return cuda_fail(ctx, e, "host copy out");
-    return STNTT_OK;
+    return host_finish(ctx, vec, d, count * 4, s);
 }
 
 int stntt_ntt_gl64_host(stntt_ctx *ctx, uint64_t *vec, uint32_t log_n, uint32_t batch, int dir) {
@@ -1324,17 +1420,15 @@ int stntt_ntt_gl64_host(stntt_ctx *ctx, uint64_t *vec, uint32_t log_n, uint32_t 
     cudaError_t e = cudaMemcpyAsync(dv, vec, count * 8, cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess)
         return cuda_fail(ctx, e, "host copy in");
+    e = cudaEventRecord(ctx->host_ev0, s);
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "cudaEventRecord");
     rc = stntt_ntt_gl64(ctx, static_cast<uint64_t *>(dv), log_n, batch, dir, s);
     if (rc) {
         cudaStreamSynchronize(s);
         return rc;
     }
-    e = cudaMemcpyAsync(vec, dv, count * 8, cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess)
-        e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess)
-        return cuda_fail(ctx, e, "host copy out");
-    return STNTT_OK;
+    return host_finish(ctx, vec, dv, count * 8, s);
 }
 
 int stntt_ntt_batch_per_call(stntt_ctx *ctx, const stntt_job *jobs, size_t njobs, stntt_stream stream) {

@@ -28,7 +28,7 @@ int run_plan(stntt_ctx *ctx, const Plan &pl, const void *in, void *out, uint64_t
 // Per-stream scratch of at least `bytes` (grows with a synchronising cudaMalloc).
 int get_workspace(stntt_ctx *ctx, cudaStream_t s, size_t bytes, void **ptr);
 // Free the workspace of a stream that is about to be destroyed.
-void release_workspace(stntt_ctx *ctx, cudaStream_t s);
+int release_workspace(stntt_ctx *ctx, cudaStream_t s);
 // Cyclic product of two length-2^log_n operands (device pointers) on stream s.
 int polymul_impl(stntt_ctx *ctx, int field, const void *a, const void *b, void *out, uint32_t log_n, uint32_t p,
                  uint64_t root, cudaStream_t s);

@@ -19,13 +19,18 @@
 //     the data region before reading it. Calls whose work overlaps on the GPU
 //     (different streams, or several host threads) race on the array; order
 //     them on one stream or synchronise between them.
-//   - The first call on a device looks up the array's device address
-//     (cudaGetSymbolAddress) with that device current; make that first call
-//     before capturing a stream into a CUDA graph.
+//   - Every call looks up the array's device address (cudaGetSymbolAddress)
+//     with the caller's device current: a host-side lookup once the library's
+//     device code is loaded, and correct again after a device reset, which
+//     places the array at a new address. CUDA loads device code lazily, so
+//     the first call on a device may load it and reserve the array and the
+//     tile kernels' code at that moment: make that first call (a warm-up)
+//     before a memory pool takes the rest of HBM and before capturing a
+//     stream into a CUDA graph. If the array cannot be placed the call
+//     returns STNTT_ENOMEM.
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <mutex>
 
 #include "../../include/stntt.h"
 #include "internal.h"
@@ -41,21 +46,17 @@ constexpr uint64_t kGlP = 0xFFFFFFFF00000001ull;
 
 static __device__ __align__(256) uint64_t g_noalloc_scratch[kDataEntries + kTableEntries];
 
-std::mutex g_addr_mu;
-uint64_t *g_addr[64] = {};  // device address of g_noalloc_scratch, per device
-
+// The device address of g_noalloc_scratch on the current device. In host
+// code the array's name stands for a host-side shadow, never a device
+// address; only this lookup gives the address kernels may use.
 int scratch_address(uint64_t **out) {
-    int dev = -1;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
-        return STNTT_ECUDA;
-    std::lock_guard<std::mutex> lk(g_addr_mu);
-    if (!g_addr[dev]) {
-        void *p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p)
-            return STNTT_ECUDA;
-        g_addr[dev] = static_cast<uint64_t *>(p);
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+        cudaGetLastError();  // clear the sticky-free error so later calls are not affected
+        return e == cudaErrorMemoryAllocation ? STNTT_ENOMEM : STNTT_ECUDA;
     }
-    *out = g_addr[dev];
+    *out = static_cast<uint64_t *>(p);
     return STNTT_OK;
 }
 
@@ -107,8 +108,9 @@ extern "C" int stntt_ntt_gl64_noalloc(const uint64_t *d_in, uint64_t *d_out, uin
         return STNTT_OK;
     }
     uint64_t *scratch = nullptr;
-    if (scratch_address(&scratch) != STNTT_OK)
-        return STNTT_ECUDA;
+    const int rc = scratch_address(&scratch);
+    if (rc != STNTT_OK)
+        return rc;
     uint64_t *data = scratch, *tables = scratch + kDataEntries;
 
     const uint64_t n = 1ull << log_n;

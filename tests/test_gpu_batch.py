@@ -140,3 +140,43 @@ def test_batched_plan_splits(ctx):
         ctx.clear_plans()
         from stntt_gb300 import tune
         tune.apply_cache(ctx)
+
+
+def test_full_reference_mix_matches_per_call(ctx):
+    """The batched configuration at full size: 4096 Goldilocks jobs, log2 n
+    uniform in [10, 18] from the benchmark's seed, alternating forward /
+    inverse (about 2.4e8 elements). The persistent launch, replayed from a
+    CUDA graph, must equal one launch sequence per transform bit for bit on
+    the same inputs; 48 jobs spread over the list are also checked against
+    the oracle."""
+    sizes = [int(v) for v in np.random.default_rng(0x57170001 + 3).integers(10, 19, 4096)]
+    total = sum(1 << s for s in sizes)
+    data = torch.empty(total, dtype=torch.int64, device="cuda")
+    st.fill_uniform_gl64(data, 4242)
+    torch.cuda.synchronize()
+    ref = data.clone()
+    jobs, jobs_ref, offs, off = [], [], [], 0
+    for i, s in enumerate(sizes):
+        jobs.append(st.Job(st.FIELD_GL64, s, i % 2, 0, 0, 0, data.data_ptr() + 8 * off))
+        jobs_ref.append(st.Job(st.FIELD_GL64, s, i % 2, 0, 0, 0, ref.data_ptr() + 8 * off))
+        offs.append(off)
+        off += 1 << s
+    sample = list(range(0, 4096, 4096 // 48))[:48]
+    inputs = {i: data[offs[i]: offs[i] + (1 << sizes[i])].cpu().numpy().view(np.uint64).copy() for i in sample}
+    b = ctx.batch_create(jobs)
+    assert b.info()["fallback_jobs"] == 0
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        b.launch(stream=s)
+    g.replay()
+    torch.cuda.synchronize()
+    assert b.status() == 0
+    ctx.ntt_batch(jobs_ref, per_call=True)
+    torch.cuda.synchronize()
+    assert torch.equal(data, ref)
+    for i in sample:
+        got = data[offs[i]: offs[i] + (1 << sizes[i])].cpu().numpy().view(np.uint64)
+        assert np.array_equal(got, O.ntt_gl64(inputs[i], inverse=bool(i % 2))), (i, sizes[i])
+    b.close()
+    del data, ref

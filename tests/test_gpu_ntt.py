@@ -149,15 +149,20 @@ def _dft_at(x, w, k, p):
 
 @pytest.mark.parametrize("lg", [24, 26])
 def test_u32_full_size(ctx, lg):
-    """u32 2^24 vs the oracle; u32 2^26: spot DFT values, linearity, round trip."""
+    """u32 2^24 and 2^26 (the large-transform sizes, exact field): forward and
+    inverse element for element against the oracle, plus spot DFT values,
+    linearity and the round trip."""
     p, root = st.params_u32(lg)
     n = 1 << lg
     x = O.uniform_u32(31, p, n)
     d = dev32(x)
     ctx.ntt_u32(d, lg, 1, p, root)
     f = host32(d)
-    if lg <= 24:
-        assert np.array_equal(f, O.ntt_u32(x, root, p))
+    assert np.array_equal(f, O.ntt_u32(x, root, p))
+    di = dev32(x)
+    ctx.ntt_u32(di, lg, 1, p, root, inverse=True)
+    assert np.array_equal(host32(di), O.ntt_u32(x, root, p, inverse=True))
+    del di
     for k in (0, 1, 12345, n - 1):
         assert int(f[k]) == _dft_at(x, root, k, p), k
     y = O.uniform_u32(32, p, n)
@@ -217,13 +222,18 @@ def test_gl64_inverse_vs_oracle(ctx):
 
 
 def test_gl64_2e24(ctx):
-    """The headline size: Goldilocks 2^24, forward vs oracle, round trip."""
+    """The headline size: Goldilocks 2^24, forward and inverse vs the oracle,
+    round trip."""
     lg = 24
     x = O.uniform_u64(2024, 1 << lg)
     d = dev64(x)
     ctx.ntt_gl64(d, lg)
     f = host64(d)
     assert np.array_equal(f, O.ntt_gl64(x, threads=1))
+    di = dev64(x)
+    ctx.ntt_gl64(di, lg, inverse=True)
+    assert np.array_equal(host64(di), O.ntt_gl64(x, inverse=True))
+    del di
     ctx.ntt_gl64(d, lg, inverse=True)
     assert np.array_equal(host64(d), x)
 
@@ -610,3 +620,46 @@ def test_cluster_path_eight_elements(ctx, field, lg, logs):
         ctx.clear_plans()
         from stntt_gb300 import tune
         tune.apply_cache(ctx)
+
+
+def test_stream_workspaces_release_and_cap(ctx):
+    """Per-stream scratch: stntt_release_stream frees a stream's buffer, and a
+    context keeps at most 64 of them (least recently used freed first)."""
+    lg = 14  # two HBM passes: a 2^14 * 8-byte workspace per stream
+    ws = (1 << lg) * 8
+    x = O.uniform_u64(3, 1 << lg)
+    want = O.ntt_gl64(x)
+    d = dev64(x)
+    ctx.ntt_gl64(d, lg)  # plan and tables for this size
+    torch.cuda.synchronize()
+    streams = [torch.cuda.Stream() for _ in range(70)]
+    base = ctx.mem_usage()
+    for i, s in enumerate(streams):
+        di = dev64(x)
+        ctx.ntt_gl64(di, lg, stream=s)
+        s.synchronize()
+        assert np.array_equal(host64(di), want), i
+    grown = ctx.mem_usage() - base
+    assert 0 < grown <= 64 * ws
+    for s in streams:
+        ctx.release_stream(s)
+    assert ctx.mem_usage() <= base
+    # still usable afterwards on a released stream
+    di = dev64(x)
+    ctx.ntt_gl64(di, lg, stream=streams[0])
+    streams[0].synchronize()
+    assert np.array_equal(host64(di), want)
+    ctx.release_stream(streams[0])
+
+
+def test_host_call_reports_kernel_time(ctx):
+    """stntt_last_kernel_ms: the device time of the last host-buffer call (what
+    the reference's autoNtt returns)."""
+    lg = 16
+    p, root = st.params_u32(lg)
+    v = O.ref_rng_vector(1 << lg)
+    ctx.ntt_stockham_host(v, 1 << lg, root, p, ref_wrap=True)
+    assert ctx.last_kernel_ms() > 0.0
+    y = O.uniform_u64(5, 1 << 20)
+    ctx.ntt_gl64_host(y, 20)
+    assert ctx.last_kernel_ms() > 0.0

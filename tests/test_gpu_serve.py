@@ -123,3 +123,36 @@ def test_admission_waits_for_memory(ctx):
         del x, y
     finally:
         sv.close()
+
+
+def test_serving_full_size_range(ctx):
+    """The serving configuration's size range, 2^12..2^22 in both fields with
+    polynomial products: a seeded trace of 40 requests at 20k requests/s. Every
+    transform is checked against the oracle, every product against the
+    oracle's cyclic convolution (forward, element-wise product, inverse), and
+    every result against the same request run alone."""
+    sv = st.Server(ctx, streams=8, max_log_n=22)
+    try:
+        reqs, arr, keep, expect = _make_trace(7, 40, 12, 22, rate=20000.0)
+        assert max(k[9] for k in keep) >= 20 and any(k[8] for k in keep)
+        comps = sv.run_trace(reqs, arr)
+        assert all(c.status == 0 for c in comps)
+        mix = [k[5].copy() for k in keep]
+        for i, (ta, tb, to, a, b, out, view, gl, poly, lg, d, p, root) in enumerate(keep):
+            res = mix[i].view(view)
+            x = a.view(view).copy()
+            if poly:
+                y = b.view(view).copy()
+                want = O.cyclic_conv_gl64(x, y) if gl else O.cyclic_conv_u32(x, y, root, p)
+                if expect[i] is not None:
+                    assert np.array_equal(want[: expect[i].size], expect[i]), i
+            else:
+                want = O.ntt_gl64(x, inverse=bool(d)) if gl else O.ntt_u32(x, root, p, inverse=bool(d))
+            assert np.array_equal(res, want), (i, lg, gl, poly)
+            out[:] = 0
+            assert sv.submit(reqs[i]) == 0
+            assert sv.wait_idle(60.0) == 0
+            assert np.array_equal(out.view(view), res), i
+        assert sv.stats()["failed"] == 0
+    finally:
+        sv.close()

@@ -153,3 +153,26 @@ def test_dft_point_matches_full_dft():
         for k in (0, 1, n // 3, n - 1):
             assert O.lib().orc_dft_point_u32(x, n, root, p, k) == full[k]
             assert O.lib().orc_dft_point_gl64(y, n, O.gl_root(lg), k) == fg[k]
+
+
+@pytest.mark.parametrize("lg", [1, 6, 10])
+def test_cyclic_conv_equals_schoolbook(golden, lg):
+    """The transform-based cyclic convolution (pwcNtt semantics) against the
+    schoolbook product folded modulo x^n - 1, both fields; also against the
+    reference's own pwc_convolution vectors."""
+    n = 1 << lg
+    root, p = O.find_params(n, 11)
+    a, b = O.uniform_u32(lg, p, n), O.uniform_u32(lg + 50, p, n)
+    full = O.polymul_u32(a, b, p).astype(np.uint64)
+    want = full[:n].copy()
+    want[: n - 1] = (want[: n - 1] + full[n:]) % p
+    assert np.array_equal(O.cyclic_conv_u32(a, b, root, p), want.astype(np.uint32))
+    x, y = O.uniform_u64(lg, n), O.uniform_u64(lg + 50, n)
+    fg = O.polymul_gl64(x, y)
+    wg = fg[:n].copy()
+    for i in range(n - 1):
+        wg[i] = (int(wg[i]) + int(fg[n + i])) % O.GL_P
+    assert np.array_equal(O.cyclic_conv_gl64(x, y), wg)
+    for c in golden["pwc"]:
+        got = O.cyclic_conv_u32(np.array(c["a"], np.uint32), np.array(c["b"], np.uint32), c["root"], c["mod"])
+        assert got.tolist() == c["out"]

@@ -3,8 +3,8 @@
 It serves callers that cannot call cudaMalloc: its scratch is a fixed array
 inside the library instead of a context workspace. Called through the C ABI
 and compared, bit for bit, with the regular entry point
-(stntt_ntt_gl64_oop) on two calls in a row. This file is named to be
-collected last.
+(stntt_ntt_gl64_oop) and with the CPU oracle, forward and inverse, single
+and batched, on two calls in a row. This file is named to be collected last.
 """
 
 import ctypes as C
@@ -49,6 +49,8 @@ def test_noalloc_matches_regular_entry_point(stntt_lib):
                     ctx.ntt_gl64_oop(src, out_regular, lg, batch, inverse=bool(inv))
                     got = _host(out_noalloc)
                     assert np.array_equal(got, _host(out_regular)), (call, lg, batch, inv)
+                    want = O.ntt_gl64(x, inverse=bool(inv), batch=batch)
+                    assert np.array_equal(got, want), (call, lg, batch, inv)
                     assert np.array_equal(_host(src), x)  # input untouched
         # in place
         x = O.uniform_u64(7, 1 << 17)
