@@ -86,6 +86,7 @@ def parse():
     ap.add_argument("--streams", type=int, default=32, help="serving: request slots")
     ap.add_argument("--serve-requests", type=int, default=0,
                     help="serving: requests in the trace (default: steps * 1000, at least 1000)")
+    ap.add_argument("--serve-rate", type=float, default=20000.0, help="serving: mean arrival rate, requests/s")
     ap.add_argument("--tma", choices=["auto", "on", "off"], default="auto",
                     help="TMA-staged passes: built-in choice per pass, everywhere allowed, or never")
     return ap.parse_args()
@@ -602,12 +603,12 @@ def run_batch_mix(args):
 SERVE_RATE, SERVE_LO, SERVE_HI, SERVE_SEED = 20000.0, 12, 22, 0x57170001 + 4
 
 
-def measure_serve(st, torch, local: int, count: int, streams: int):
+def measure_serve(st, torch, local: int, count: int, streams: int, rate: float = SERVE_RATE):
     """Seeded Poisson stream (mean 20k requests/s): 70% single NTTs, 30%
     cyclic polynomial products of two polynomials of degree < n/2, n = 2^k with
     k uniform in [12, 22], 50/50 32-bit prime / Goldilocks."""
     rng = np.random.default_rng(SERVE_SEED)
-    arrivals = np.cumsum(rng.exponential(1.0 / SERVE_RATE, count))
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, count))
     kinds = rng.random(count) < 0.3
     logs = rng.integers(SERVE_LO, SERVE_HI + 1, count)
     gls = rng.integers(0, 2, count).astype(bool)
@@ -659,7 +660,7 @@ def measure_serve(st, torch, local: int, count: int, streams: int):
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p90": float(np.percentile(lat, 90)),
                        "p99": float(np.percentile(lat, 99)), "max": float(lat.max()),
                        "queue_p50": float(np.percentile(qwait, 50)), "queue_p99": float(np.percentile(qwait, 99))},
-        "throughput": {"requests_per_s": count / span, "offered_per_s": SERVE_RATE,
+        "throughput": {"requests_per_s": count / span, "offered_per_s": rate,
                        "transform_gelem_per_s": elems / span / 1e9, "span_s": span, "wall_s": wall},
         "requests": count, "server": stats, "status_ok": ok}
 
@@ -674,7 +675,7 @@ def run_serve_mix(args):
     sampler = ClockSampler(gpu_index(local))
     sampler.start()
     time.sleep(0.25)
-    m = measure_serve(st, torch, local, count, args.streams)
+    m = measure_serve(st, torch, local, count, args.streams, args.serve_rate)
     clocks = sampler.stop()
     if rank == 0:
         print(json.dumps({
@@ -682,7 +683,7 @@ def run_serve_mix(args):
             "value": m["latency_ms"]["p99"], "unit": "ms (p99 latency)", "higher_is_better": False,
             "n_gpus": world, "steps": args.steps, "warmup": 200, "ms_per_step": None, "scaling": "weak",
             "vs_baseline": None, "dtype": "u32+u64", "data": "synthetic (splitmix64 residues, seeded Poisson trace)",
-            "config": {"workload": "serve_mix", "requests": count, "rate_per_s": SERVE_RATE,
+            "config": {"workload": "serve_mix", "requests": count, "rate_per_s": args.serve_rate,
                        "log_n_range": [SERVE_LO, SERVE_HI], "polymul_fraction": 0.3, "fields": "50/50",
                        "streams": args.streams, "seed": SERVE_SEED},
             "latency_ms": m["latency_ms"], "throughput": m["throughput"], "server": m["server"], "clocks": clocks,

@@ -108,9 +108,17 @@ int stntt_plan_info(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t p, uint3
 int stntt_call_info(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t batch, uint32_t p, uint32_t root, int dir,
                     uint32_t *launches, uint32_t *pass_logs);
 
+/* elems flag: run the pass with the vector-lines build (V adjacent lines per
+ * thread, 16-byte loads and stores; passes of multi-pass plans with tiles of
+ * 2^7..2^10 points, 16 points per line, or 8 with elems = 8 | STNTT_PASS_VEC);
+ * cols then gives the lines per CTA (4 or 8 times V, V = 4 for the 32-bit
+ * field and 2 for Goldilocks). */
+#define STNTT_PASS_VEC 0x100u
+
 /* Override the plan for one (field, log_n): npasses HBM passes (1..4) with
  * tile lengths 2^pass_logs[i] (summing to log_n, each <= 13; npasses <= 3), elements per
- * thread elems[i] (16 or 32, or 8 for tiles of 2^7..2^11 points; 0 = default) and columns per CTA cols[i] (a power
+ * thread elems[i] (16 or 32, or 8 for tiles of 2^7..2^11 points; 0 = default; may carry
+ * STNTT_PASS_VEC) and columns per CTA cols[i] (a power
  * of two; 0 = default). Drops cached plans of that size. The autotuner
  * (stntt_gb300/tune.py) drives this and stores its choices on disk.
  * stntt_clear_plans() restores the built-in defaults for every size. */
@@ -225,6 +233,14 @@ int stntt_set_tma(stntt_ctx *ctx, int mode);
  * (after about a second) since the last call -- its output is then
  * incomplete -- else STNTT_OK. Reads a device word: synchronise the streams
  * that ran the transforms first. Clears the word. */
+/* Small calls (fewer than 2^22 elements) of a two-pass plan of 2^18..2^21
+ * points may run both passes in one cooperative launch (a grid-wide barrier
+ * between the passes, bounded like every device-side wait): 1 where the shape
+ * fits, 0 (default) never, i.e. two launches, which measured faster on GB300
+ * at every such size. No counterpart in the reference, which launches every
+ * stage separately and synchronises the host between them
+ * (src/cuda/ntt/implementations/st_ntt_global_radix2.cuh:104-113). */
+int stntt_set_coop(stntt_ctx *ctx, int mode);
 int stntt_device_status(stntt_ctx *ctx);
 /* Launch the staged kernel with no copy issued, so that its first wait runs
  * out after spin_limit polls; returns STNTT_ETIMEOUT when the kernel reported
@@ -277,6 +293,13 @@ typedef struct stntt_server_config {
 typedef struct stntt_server_stats {
     uint64_t submitted, admitted, completed, failed, rejected;
     uint64_t peak_inflight, arena_bytes, peak_arena_used;
+    /* scheduler-thread time: issuing admitted requests (copies, kernels,
+     * events) and checking slots for completion, in nanoseconds */
+    uint64_t issue_ns, poll_ns;
+    /* stntt_server_run_trace only: the latest a request was handed to the
+     * server after its arrival time (the load driver's own lag, counted in
+     * the request's latency), and how many were more than 0.5 ms late */
+    uint64_t trace_late_max_ns, trace_late_count;
 } stntt_server_stats;
 typedef struct stntt_server stntt_server;
 double stntt_clock_s(void);

@@ -29,7 +29,7 @@ import numpy as np
 
 __all__ = [
     "StnttError", "lib", "Context", "findParams", "params_u32", "gl64_root", "nttStockham",
-    "GL_P", "FORWARD", "INVERSE", "FIELD_U32", "FIELD_GL64", "FLAG_REF_WRAP", "Job",
+    "GL_P", "FORWARD", "INVERSE", "FIELD_U32", "FIELD_GL64", "FLAG_REF_WRAP", "PASS_VEC", "Job",
 ]
 
 PKG = Path(__file__).resolve().parent
@@ -38,6 +38,7 @@ GL_P = 0xFFFFFFFF00000001
 FORWARD, INVERSE = 0, 1
 FIELD_U32, FIELD_GL64 = 0, 1
 FLAG_REF_WRAP = 0x1
+PASS_VEC = 0x100  # STNTT_PASS_VEC: elems flag for the vector-lines build of a pass
 STATUS = {0: "OK", 1: "EINVAL", 2: "ENOMEM", 3: "ECUDA", 4: "ETIMEOUT", 5: "EUNSUPPORTED"}
 
 
@@ -74,7 +75,8 @@ class ServerConfig(C.Structure):
 
 class ServerStats(C.Structure):
     _fields_ = [(k, C.c_uint64) for k in ("submitted", "admitted", "completed", "failed", "rejected",
-                                          "peak_inflight", "arena_bytes", "peak_arena_used")]
+                                          "peak_inflight", "arena_bytes", "peak_arena_used", "issue_ns", "poll_ns",
+                                          "trace_late_max_ns", "trace_late_count")]
 
 
 REQ_NTT, REQ_POLYMUL = 0, 1
@@ -126,6 +128,7 @@ _SIGS = {
     "stntt_batch_destroy": (_int, [_vp]),
     "stntt_selftest_wait_timeout": (_int, [_vp, _u32]),
     "stntt_set_tma": (_int, [_vp, _int]),
+    "stntt_set_coop": (_int, [_vp, _int]),
     "stntt_device_status": (_int, [_vp]),
     "stntt_selftest_tma_timeout": (_int, [_vp, _u32]),
     "stntt_clock_s": (C.c_double, []),
@@ -335,6 +338,11 @@ class Context:
         """TMA-staged passes: -1 built-in choice, 0 never, 1 wherever a pass
         allows it (stntt_set_tma; drops cached plans)."""
         _check(lib().stntt_set_tma(self._h, mode), self._h)
+
+    def set_coop(self, mode: int) -> None:
+        """Small two-pass calls of 2^18..2^21 points as one cooperative launch:
+        1 where the shape fits (default), 0 never (stntt_set_coop)."""
+        _check(lib().stntt_set_coop(self._h, mode), self._h)
 
     def device_status(self) -> int:
         """STNTT_ETIMEOUT (4) when a staged pass gave up waiting for a copy

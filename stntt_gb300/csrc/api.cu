@@ -94,6 +94,26 @@ uint64_t host_tw_entry(int field, uint64_t w, uint32_t p) {
     return (w & 0xffffffffull) | (wp << 32);
 }
 
+cudaError_t launch_tile_vec_gl64(const PassDesc &, const void *, const void *, void *, uint64_t, cudaStream_t);
+cudaError_t launch_tile_vec_u32l(const PassDesc &, uint32_t, const void *, const void *, void *, uint64_t,
+                                 cudaStream_t);
+cudaError_t preload_vec_gl64();
+cudaError_t preload_vec_u32l();
+
+cudaError_t launch_tile_vec(int field, const PassDesc &d, uint32_t p, const void *tables, const void *in, void *out,
+                            uint64_t batch, cudaStream_t s) {
+    if (field == kFieldGL)
+        return launch_tile_vec_gl64(d, tables, in, out, batch, s);
+    if (p < (1u << 30))  // the lazy 32-bit field (every findParams prime up to 2^26)
+        return launch_tile_vec_u32l(d, p, tables, in, out, batch, s);
+    return cudaErrorNotSupported;
+}
+
+cudaError_t preload_vec() {
+    const cudaError_t e = preload_vec_gl64();
+    return e == cudaSuccess ? preload_vec_u32l() : e;
+}
+
 cudaError_t preload_kernels() {
     cudaError_t e = preload_u32();
     if (e == cudaSuccess)
@@ -104,11 +124,18 @@ cudaError_t preload_kernels() {
         e = preload_tma_u32l();
     if (e == cudaSuccess)
         e = preload_tma_gl64();
+    if (e == cudaSuccess)
+        e = preload_vec();
     return e;
 }
 
 cudaError_t launch_tile(int field, const PassDesc &d, uint32_t p, const void *tables, const void *in, void *out,
                         uint64_t batch, cudaStream_t s, const void *in2, int *err) {
+    if (d.vec && !in2) {  // the vector-lines build where the pass and its pointers allow it
+        const cudaError_t e = launch_tile_vec(field, d, p, tables, in, out, batch, s);
+        if (e != cudaErrorNotSupported)
+            return e;
+    }
     if (field == kFieldGL)
         return launch_tile_gl64(d, p, tables, in, out, batch, s, in2, err);
     // lazy reduction needs 4p < 2^32
@@ -231,6 +258,9 @@ struct StreamBuf {
 // Streams whose scratch a context keeps at once (the serving loop uses one
 // per slot, up to 32); beyond this the least recently used buffer is freed.
 constexpr size_t kMaxStreamWorkspaces = 64;
+// Bytes after each stream's scratch, zeroed when it is allocated: the grid
+// barrier of the one-launch two-pass kernel (coop.cuh).
+constexpr size_t kWorkspaceTail = 256;
 
 // A plan shape chosen by the caller (the autotuner) instead of the default.
 struct PlanSpec {
@@ -261,6 +291,7 @@ struct stntt_ctx {
     size_t mem = 0;
     uint32_t cluster_log = 3;  // log2 of the cluster size the one-launch transforms use (3 or 4)
     int tma_mode = -1;         // TMA-staged passes: -1 built-in choice, 0 never, 1 wherever a pass allows
+    int coop_mode = 0;         // one cooperative launch for small two-pass calls: 1 where it fits, 0 never
     int *d_err = nullptr;      // device error word of the staged kernels' bounded waits
 };
 
@@ -367,6 +398,36 @@ void shape_pass(PassDesc &d, int field, uint64_t col_limit, uint32_t want_E, uin
     d.smem_bytes = (size_t)C * d.cs * (field == kFieldGL ? 8 : 4);
 }
 
+// The vector-lines build of a pass (tile_v.cuh), when asked for (STNTT_PASS_VEC
+// in a plan's elements per thread) and the pass allows it: a pass of a
+// multi-pass plan with a tile of 2^7..2^10 points, E = 16 (or 8) points per
+// line per thread, V = 16 bytes / w lines per thread and C = V * 2^g lines per
+// CTA (g = 2 or 3), C dividing the pass's lines per sub-problem. want_C picks
+// C (0: 8 line groups where they fit, else 4).
+void shape_pass_vec(PassDesc &d, int field, uint64_t col_limit, uint32_t want_E, uint32_t want_C) {
+    d.vec = 0;
+    if (d.logL < 7 || d.logL > 10 || d.do_scale || d.logL >= d.logN)
+        return;
+    const uint32_t V = field == kFieldGL ? 2 : 4, w = field == kFieldGL ? 8 : 4;
+    d.vE = want_E == 8 ? 8 : 16;
+    const uint32_t U = (1u << d.logL) / d.vE;
+    uint32_t logG = 3;
+    if (want_C >= 4 * V && want_C <= 8 * V)
+        logG = want_C >= 8 * V ? 3 : 2;
+    while (logG >= 2 && ((uint64_t)V << logG) > col_limit)
+        --logG;
+    while (logG > 2 && (((size_t)V << logG) * (1u << d.logL) * w > 200 * 1024 || (U << logG) > 1024))
+        --logG;
+    if (logG < 2 || ((uint64_t)V << logG) > col_limit || (U << logG) > 1024)
+        return;
+    d.vec = V;
+    d.vlogG = logG;
+    d.vthreads = U << logG;
+    d.vsmem = ((size_t)V << logG) * (1u << d.logL) * w;
+    if (d.vsmem > 200 * 1024)
+        d.vec = 0;
+}
+
 // Whether a pass runs TMA-staged (tma.cuh) by default; the kernel still
 // falls back to the plain one where the pass does not allow it.
 uint32_t tma_builtin(int field, const PassDesc &d) {
@@ -400,21 +461,24 @@ int build_plan(stntt_ctx *ctx, Plan &pl, int field, uint32_t log_n, uint32_t p, 
     // base, scale), or a column pass's full four-step table (built from its
     // lo / hi tables, which come earlier).
     struct TableReq {
-        uint64_t count, base, scale;
+        uint64_t at, count, base, scale;
         bool full;
         uint64_t lo_off, hi_off;
         uint32_t h, logS;
     };
     std::vector<TableReq> reqs;
     uint64_t off = 0;
+    // every table starts on a 32-byte boundary (vector loads of 2 or 4 entries)
     auto add_table = [&](uint64_t count, uint64_t base, uint64_t scale) {
-        reqs.push_back({count, base, scale, false, 0, 0, 0, 0});
+        off = (off + 3) & ~3ull;
+        reqs.push_back({off, count, base, scale, false, 0, 0, 0, 0});
         const uint64_t o = off;
         off += count;
         return o;
     };
     auto add_full = [&](uint64_t count, uint64_t lo_off, uint64_t hi_off, uint32_t h, uint32_t logS) {
-        reqs.push_back({count, 0, 0, true, lo_off, hi_off, h, logS});
+        off = (off + 3) & ~3ull;
+        reqs.push_back({off, count, 0, 0, true, lo_off, hi_off, h, logS});
         const uint64_t o = off;
         off += count;
         return o;
@@ -465,7 +529,13 @@ int build_plan(stntt_ctx *ctx, Plan &pl, int field, uint32_t log_n, uint32_t p, 
             d.logN2 = K == 3 ? logs[1] : 0;
             col_limit = 1ull << 20;
         }
-        shape_pass(d, field, col_limit, spec ? spec->elems[i] : 0, spec ? spec->cols[i] : 0);
+        const uint32_t want_e = spec ? spec->elems[i] : 0;
+        shape_pass(d, field, col_limit, want_e & 0xffu, (want_e & STNTT_PASS_VEC) ? 0 : (spec ? spec->cols[i] : 0));
+        if (K > 1 && (want_e & STNTT_PASS_VEC)) {
+            if (d.mode == kModeRow)
+                col_limit = std::min<uint64_t>(col_limit, 1ull << (log_n - d.logL));
+            shape_pass_vec(d, field, col_limit, want_e & 0xffu, spec ? spec->cols[i] : 0);
+        }
         d.tma = ctx->tma_mode < 0 ? tma_builtin(field, d) : (uint32_t)ctx->tma_mode;
         pl.passes.push_back(d);
         done += d.logL;
@@ -477,15 +547,13 @@ int build_plan(stntt_ctx *ctx, Plan &pl, int field, uint32_t log_n, uint32_t p, 
         pl.d_tables = nullptr;
         return cuda_fail(ctx, e, "cudaMalloc(twiddle tables)");
     }
-    uint64_t o = 0;
     char *tb = static_cast<char *>(pl.d_tables);
     for (const auto &r : reqs) {
-        e = r.full ? launch_gen_four_step(field, tb + o * esz, tb + r.lo_off * esz, tb + r.hi_off * esz, r.h, r.logS,
-                                          r.count, p, ctx->setup)
-                   : launch_gen_powers(field, tb + o * esz, r.count, r.base, r.scale, p, ctx->setup);
+        e = r.full ? launch_gen_four_step(field, tb + r.at * esz, tb + r.lo_off * esz, tb + r.hi_off * esz, r.h,
+                                          r.logS, r.count, p, ctx->setup)
+                   : launch_gen_powers(field, tb + r.at * esz, r.count, r.base, r.scale, p, ctx->setup);
         if (e != cudaSuccess)
             return cuda_fail(ctx, e, "twiddle generation launch");
-        o += r.count;
     }
     e = cudaStreamSynchronize(ctx->setup);
     if (e != cudaSuccess)
@@ -536,7 +604,7 @@ int get_plan(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t p, uint64_t roo
 // least recently used one when a stream beyond kMaxStreamWorkspaces appears,
 // is taken out of the map under the lock and waited for and freed outside it,
 // so other threads on the context do not stall behind that wait.
-int get_workspace(stntt_ctx *ctx, cudaStream_t s, size_t bytes, void **ptr) {
+int get_workspace(stntt_ctx *ctx, cudaStream_t s, size_t bytes, void **ptr, void **tail) {
     StreamBuf old, victim;
     cudaStream_t victim_s = nullptr;
     {
@@ -545,6 +613,8 @@ int get_workspace(stntt_ctx *ctx, cudaStream_t s, size_t bytes, void **ptr) {
         if (it != ctx->workspaces.end() && it->second.buf.bytes >= bytes) {
             it->second.last_use = ++ctx->ws_clock;
             *ptr = it->second.buf.ptr;
+            if (tail)
+                *tail = static_cast<char *>(it->second.buf.ptr) + it->second.buf.bytes;
             return STNTT_OK;
         }
         if (it != ctx->workspaces.end()) {
@@ -559,7 +629,8 @@ int get_workspace(stntt_ctx *ctx, cudaStream_t s, size_t bytes, void **ptr) {
             victim_s = lru->first;
             ctx->workspaces.erase(lru);
         }
-        ctx->mem -= old.buf.bytes + victim.buf.bytes;
+        ctx->mem -= (old.buf.ptr ? old.buf.bytes + kWorkspaceTail : 0) +
+                    (victim.buf.ptr ? victim.buf.bytes + kWorkspaceTail : 0);
     }
     if (old.buf.ptr) {
         const cudaError_t e = cudaStreamSynchronize(s);
@@ -575,10 +646,16 @@ int get_workspace(stntt_ctx *ctx, cudaStream_t s, size_t bytes, void **ptr) {
         cudaFree(victim.buf.ptr);
     }
     StreamBuf nb;
-    const cudaError_t e = cudaMalloc(&nb.buf.ptr, bytes);
+    bytes = (bytes + 255) & ~(size_t)255;
+    cudaError_t e = cudaMalloc(&nb.buf.ptr, bytes + kWorkspaceTail);
     if (e != cudaSuccess)
         return fail(ctx, e == cudaErrorMemoryAllocation ? STNTT_ENOMEM : STNTT_ECUDA,
                     std::string("cudaMalloc(workspace): ") + cudaGetErrorString(e));
+    e = cudaMemset(static_cast<char *>(nb.buf.ptr) + bytes, 0, kWorkspaceTail);
+    if (e != cudaSuccess) {
+        cudaFree(nb.buf.ptr);
+        return cuda_fail(ctx, e, "workspace tail");
+    }
     nb.buf.bytes = bytes;
     std::lock_guard<std::mutex> g(ctx->mu);
     nb.last_use = ++ctx->ws_clock;
@@ -587,16 +664,20 @@ int get_workspace(stntt_ctx *ctx, cudaStream_t s, size_t bytes, void **ptr) {
         if (ins.first->second.buf.bytes >= bytes) {
             cudaFree(nb.buf.ptr);
             *ptr = ins.first->second.buf.ptr;
+            if (tail)
+                *tail = static_cast<char *>(ins.first->second.buf.ptr) + ins.first->second.buf.bytes;
             return STNTT_OK;
         }
         // both were ordered on this stream: the smaller one is idle once the stream is
         cudaStreamSynchronize(s);
         cudaFree(ins.first->second.buf.ptr);
-        ctx->mem -= ins.first->second.buf.bytes;
+        ctx->mem -= ins.first->second.buf.bytes + kWorkspaceTail;
         ins.first->second = nb;
     }
-    ctx->mem += bytes;
+    ctx->mem += bytes + kWorkspaceTail;
     *ptr = nb.buf.ptr;
+    if (tail)
+        *tail = static_cast<char *>(nb.buf.ptr) + bytes;
     return STNTT_OK;
 }
 
@@ -665,6 +746,54 @@ bool cluster_shape(const stntt_ctx *ctx, const Plan &pl, ClusterShape &cs) {
            cluster_shape(pl, kClusterLogSmall, cs);
 }
 
+// A two-pass plan's passes as one cooperative launch (coop.cuh): both passes
+// reshaped to 8 points per thread and one block size (the larger pass's
+// threads per line, at least 256). false when the shape does not fit (tiles
+// of 2^8..2^11 points, 2^18..2^21-point transforms, no full four-step table,
+// a prime with the lazy kernels).
+struct CoopShape {
+    PassDesc d1, d2;
+    size_t smem = 0;
+};
+
+bool coop_shape(const Plan &pl, CoopShape &cs) {
+    if (pl.passes.size() != 2 || (pl.field != kFieldGL && pl.p >= (1u << 30)))
+        return false;
+    const PassDesc &p1 = pl.passes[0], &p2 = pl.passes[1];
+    if (p1.mode != kModeCol || p2.mode != kModeRow || p1.full_off != ~0ull || p1.logL < 8 || p1.logL > 11 ||
+        p2.logL < 8 || p2.logL > 11 || pl.log_n < 18 || pl.log_n > 21)
+        return false;
+    const uint32_t u1 = (1u << p1.logL) / 8, u2 = (1u << p2.logL) / 8;
+    const uint32_t T = std::max<uint32_t>(256, std::max(u1, u2));
+    if (T > 512 || T / u1 > (1u << p1.logS) || T / u2 > (1u << (pl.log_n - p2.logL)))
+        return false;
+    cs.d1 = p1;
+    cs.d2 = p2;
+    cs.d1.vec = cs.d2.vec = 0;
+    shape_pass(cs.d1, pl.field, 1ull << p1.logS, 8, T / u1);
+    shape_pass(cs.d2, pl.field, 1ull << (pl.log_n - p2.logL), 8, T / u2);
+    if (cs.d1.E != 8 || cs.d2.E != 8 || cs.d1.threads != T || cs.d2.threads != T)
+        return false;
+    cs.smem = std::max(cs.d1.smem_bytes, cs.d2.smem_bytes);
+    return cs.smem <= 200 * 1024;
+}
+
+int run_coop(stntt_ctx *ctx, const Plan &pl, const void *in, void *out, uint64_t batch, cudaStream_t s) {
+    CoopShape cs;
+    if (ctx->coop_mode == 0 || !coop_shape(pl, cs))
+        return STNTT_EUNSUPPORTED;
+    const size_t bytes = (batch << pl.log_n) * (pl.field == kFieldGL ? 8 : 4);
+    void *ws = nullptr, *tail = nullptr;
+    const int rc = get_workspace(ctx, s, bytes, &ws, &tail);
+    if (rc)
+        return rc;
+    const cudaError_t e = launch_coop(pl.field, cs.d1, cs.d2, pl.p, pl.d_tables, in, ws, out, batch, cs.smem, tail,
+                                      ctx->d_err, s);
+    if (e == cudaErrorNotSupported)
+        return STNTT_EUNSUPPORTED;
+    return e == cudaSuccess ? STNTT_OK : cuda_fail(ctx, e, "cooperative launch");
+}
+
 int run_cluster(stntt_ctx *ctx, const Plan &pl, const void *in, void *out, uint64_t batch, cudaStream_t s) {
     ClusterShape cs;
     if (!cluster_shape(ctx, pl, cs))
@@ -694,8 +823,11 @@ int run_plan(stntt_ctx *ctx, const Plan &pl, const void *in, void *out, uint64_t
         return STNTT_OK;
     }
     if (!in2 && pl.passes.size() == 2 && ((uint64_t)batch << pl.log_n) < kSmallCallElems) {
-        // Small two-pass calls: both passes in one cluster launch (cluster.cuh).
-        const int rc = run_cluster(ctx, pl, in, out, batch, s);
+        // Small two-pass calls: both passes in one cluster launch (cluster.cuh)
+        // up to 2^17 points, else in one cooperative launch (coop.cuh).
+        int rc = run_cluster(ctx, pl, in, out, batch, s);
+        if (rc == STNTT_EUNSUPPORTED)
+            rc = run_coop(ctx, pl, in, out, batch, s);
         if (rc != STNTT_EUNSUPPORTED)
             return rc;
     }
@@ -862,7 +994,7 @@ int release_workspace(stntt_ctx *ctx, cudaStream_t s) {
         if (it == ctx->workspaces.end())
             return STNTT_OK;
         b = it->second;
-        ctx->mem -= b.buf.bytes;
+        ctx->mem -= b.buf.bytes + kWorkspaceTail;
         ctx->workspaces.erase(it);
     }
     const cudaError_t e = cudaStreamSynchronize(s);
@@ -1110,8 +1242,9 @@ int set_plan_for(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t npasses, co
         const uint32_t lg = pass_logs[i], e = elems ? elems[i] : 0, c = cols ? cols[i] : 0;
         if (lg == 0 || lg > 13)
             return fail(ctx, STNTT_EINVAL, "set_plan: each pass length must be 2^1..2^13");
-        if (e != 0 && e != 8 && e != 16 && e != 32)
-            return fail(ctx, STNTT_EINVAL, "set_plan: elems must be 0, 8, 16 or 32");
+        const uint32_t eb = e & ~STNTT_PASS_VEC;
+        if ((eb != 0 && eb != 8 && eb != 16 && eb != 32) || ((e & STNTT_PASS_VEC) && eb == 32))
+            return fail(ctx, STNTT_EINVAL, "set_plan: elems must be 0, 8, 16 or 32 (STNTT_PASS_VEC with 0, 8 or 16)");
         if (c & (c - 1))
             return fail(ctx, STNTT_EINVAL, "set_plan: cols must be 0 or a power of two");
         s.logs.push_back(lg);
@@ -1169,8 +1302,10 @@ int stntt_call_info(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t batch, u
     if (rc)
         return rc;
     ClusterShape cs;
-    const bool cluster = ((uint64_t)batch << log_n) < kSmallCallElems && cluster_shape(ctx, *pl, cs);
-    *launches = cluster ? 1u : (uint32_t)pl->passes.size();
+    CoopShape co;
+    const bool small = ((uint64_t)batch << log_n) < kSmallCallElems;
+    const bool one = small && (cluster_shape(ctx, *pl, cs) || (ctx->coop_mode != 0 && coop_shape(*pl, co)));
+    *launches = one ? 1u : (uint32_t)pl->passes.size();
     if (pass_logs)
         for (size_t i = 0; i < pl->passes.size() && i < 4; ++i)
             pass_logs[i] = pl->passes[i].logL;
@@ -1234,6 +1369,14 @@ int stntt_set_tma(stntt_ctx *ctx, int mode) {
     return STNTT_OK;
 }
 
+int stntt_set_coop(stntt_ctx *ctx, int mode) {
+    if (!ctx || mode < 0 || mode > 1)
+        return STNTT_EINVAL;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->coop_mode = mode;
+    return STNTT_OK;
+}
+
 int stntt_device_status(stntt_ctx *ctx) {
     if (!ctx)
         return STNTT_EINVAL;
@@ -1244,8 +1387,17 @@ int stntt_device_status(stntt_ctx *ctx) {
         e = cudaMemset(ctx->d_err, 0, sizeof(int));
     if (e != cudaSuccess)
         return cuda_fail(ctx, e, "reading the device error word");
-    if (flag)
-        return fail(ctx, STNTT_ETIMEOUT, "a TMA-staged pass gave up waiting for its copy (its output is incomplete)");
+    if (flag) {
+        // a bounded wait ran out: clear every stream's barrier words, which a
+        // cooperative launch that gave up may have left mid-count
+        cudaDeviceSynchronize();
+        std::lock_guard<std::mutex> lk(ctx->mu);
+        for (auto &kv : ctx->workspaces)
+            cudaMemset(static_cast<char *>(kv.second.buf.ptr) + kv.second.buf.bytes, 0, kWorkspaceTail);
+        ctx->err = "a device-side wait gave up (a TMA-staged copy or the grid barrier of a cooperative launch); "
+                   "that call's output is incomplete";
+        return STNTT_ETIMEOUT;
+    }
     return STNTT_OK;
 }
 

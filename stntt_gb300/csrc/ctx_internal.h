@@ -25,8 +25,9 @@ int get_plan(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t p, uint64_t roo
 // in2: optional second input whose product with `in` the first pass transforms.
 int run_plan(stntt_ctx *ctx, const Plan &pl, const void *in, void *out, uint64_t batch, cudaStream_t s,
              const void *in2 = nullptr);
-// Per-stream scratch of at least `bytes` (grows with a synchronising cudaMalloc).
-int get_workspace(stntt_ctx *ctx, cudaStream_t s, size_t bytes, void **ptr);
+// Per-stream scratch of at least `bytes` (grows with a synchronising cudaMalloc);
+// *tail (optional): 256 zero-initialised bytes after it that belong to the stream.
+int get_workspace(stntt_ctx *ctx, cudaStream_t s, size_t bytes, void **ptr, void **tail = nullptr);
 // Free the workspace of a stream that is about to be destroyed.
 int release_workspace(stntt_ctx *ctx, cudaStream_t s);
 // Cyclic product of two length-2^log_n operands (device pointers) on stream s.

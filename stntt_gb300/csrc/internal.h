@@ -35,6 +35,14 @@ struct PassDesc {
     uint64_t wR[8] = {};      // raw twiddle entries (u32: {w, w'} packed little-endian)
     uint64_t scale = 0;       // raw twiddle entry
     uint32_t tma = 0;         // 1: run as the TMA-staged persistent kernel where the pass allows it (tma.cuh)
+    // The vector-lines build (tile_v.cuh) of this pass, when vec != 0: vec
+    // lines per thread (4 four-byte or 2 eight-byte), vE points per line per
+    // thread, 2^vlogG line groups per CTA, vthreads threads and vsmem bytes of
+    // shared memory. The fields above
+    // keep the plain build's shape, which runs where the vector build cannot
+    // (unaligned pointers, a prime of 2^30 or more).
+    uint32_t vec = 0, vE = 16, vlogG = 0, vthreads = 0;
+    size_t vsmem = 0;
 };
 
 // ---- launchers (return the CUDA error of the launch) ----------------------
@@ -57,6 +65,18 @@ cudaError_t launch_cluster(int field, const PassDesc &d1, const PassDesc &d2, ui
                            uint32_t log_k, cudaStream_t s);
 // Largest cluster the current device schedules for the cluster kernels (8 or 16).
 int cluster_max_size();
+// The vector-lines build of a pass (tile_v.cuh); cudaErrorNotSupported when
+// the pass or its pointers do not allow it (the caller then runs the plain one).
+cudaError_t launch_tile_vec(int field, const PassDesc &d, uint32_t p, const void *tables, const void *in, void *out,
+                            uint64_t batch, cudaStream_t s);
+cudaError_t preload_vec();
+// Both passes of a two-pass plan in one cooperative launch (coop.cuh): d1 the
+// column pass into ws, d2 the row pass into out, with equal block sizes; bar:
+// the stream's zero-initialised barrier words; err: the device error word.
+// cudaErrorNotSupported when the shape is not instantiated or not resident.
+cudaError_t launch_coop(int field, const PassDesc &d1, const PassDesc &d2, uint32_t p, const void *tables,
+                        const void *in, void *ws, void *out, uint64_t batch, size_t smem, void *bar, int *err,
+                        cudaStream_t s);
 // out[pos * 2^logS + col] = w_M^(col * pos) for count = M entries, from the
 // two-level tables lo (w_M^e, e < 2^h) and hi (s * w_M^(e 2^h)).
 cudaError_t launch_gen_four_step(int field, void *out, const void *lo, const void *hi, uint32_t h, uint32_t logS,

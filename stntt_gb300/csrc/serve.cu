@@ -230,6 +230,7 @@ void scheduler(stntt_server *sv) {
             }
         }
         bool progress = false, busy = false;
+        const double t_poll = now_s();
         // completions
         for (Slot &sl : sv->slots) {
             if (!sl.busy)
@@ -243,6 +244,11 @@ void scheduler(stntt_server *sv) {
             sl.busy = false;
             complete(sv, sl.req, q == cudaSuccess ? STNTT_OK : STNTT_ECUDA);
             progress = true;
+        }
+        double t_issue = now_s();
+        {
+            std::lock_guard<std::mutex> lk(sv->mu);
+            sv->stats.poll_ns += (uint64_t)((t_issue - t_poll) * 1e9);
         }
         // admissions, in arrival order
         while (!sv->pending.empty()) {
@@ -280,6 +286,12 @@ void scheduler(stntt_server *sv) {
                 free_slot->busy = false;
                 complete(sv, free_slot->req, rc);
             }
+            const double t = now_s();
+            {
+                std::lock_guard<std::mutex> lk(sv->mu);
+                sv->stats.issue_ns += (uint64_t)((t - t_issue) * 1e9);
+            }
+            t_issue = t;
         }
         if (sv->stop.load() && sv->pending.empty() && !busy && !progress) {
             std::lock_guard<std::mutex> lk(sv->mu);
@@ -349,13 +361,23 @@ int stntt_server_create(stntt_ctx *ctx, const stntt_server_config *cfg, stntt_se
             return STNTT_ENOMEM;
         }
     }
-    // resident twiddle tables for both fields, both directions, the size range
+    // resident twiddle tables for both fields, both directions, the size range:
+    // the very plans a request of that size looks up (a request is one call of
+    // one transform, so sizes below 2^22 take the small-call plans). A plan
+    // built in the middle of a trace stalls the scheduler thread while its
+    // tables are allocated and generated.
     for (uint32_t lg = c.prewarm_min_log_n; c.prewarm_max_log_n && lg <= c.prewarm_max_log_n; ++lg) {
+        const int kind = (1ull << lg) < sd::kSmallCallElems ? sd::kPlanSmall : sd::kPlanAll;
         for (int dir = 0; dir < 2; ++dir) {
             uint32_t p32 = 0, r32 = 0;
-            int rc = stntt_prepare(ctx, STNTT_FIELD_GL64, lg, 0, 0, dir);
-            if (!rc && !stntt_params_u32(lg, &p32, &r32))
-                rc = stntt_prepare(ctx, STNTT_FIELD_U32, lg, p32, r32, dir);
+            uint64_t rg = 0;
+            const sd::Plan *pl = nullptr;
+            stntt_gl64_root(lg, &rg);
+            int rc = sd::get_plan(ctx, stntt::kFieldGL, lg, 0, rg, dir, &pl, kind);
+            if (!rc)
+                rc = stntt_params_u32(lg, &p32, &r32);
+            if (!rc)
+                rc = sd::get_plan(ctx, stntt::kFieldU32, lg, p32, r32, dir, &pl, kind);
             if (rc) {
                 stntt_server_destroy(sv.release());
                 return rc;
@@ -435,11 +457,21 @@ int stntt_server_run_trace(stntt_server *sv, const stntt_request *reqs, const do
     if (!sv || (n && (!reqs || !arrival_s || !out)))
         return STNTT_EINVAL;
     const double t0 = now_s() + 1e-3;
+    double late_max = 0;
+    uint64_t late_count = 0;
     for (size_t i = 0; i < n; ++i) {
         const double t = t0 + arrival_s[i];
-        while (now_s() < t) {
+        double now;
+        while ((now = now_s()) < t) {
         }
+        late_max = std::max(late_max, now - t);
+        late_count += now - t > 0.5e-3;
         stntt_server_submit_at(sv, &reqs[i], t);
+    }
+    {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        sv->stats.trace_late_max_ns = std::max<uint64_t>(sv->stats.trace_late_max_ns, (uint64_t)(late_max * 1e9));
+        sv->stats.trace_late_count += late_count;
     }
     int rc = stntt_server_wait_idle(sv, timeout_s);
     // gather: completions carry the request ids; place by position among reqs

@@ -1,0 +1,275 @@
+// tile_v.cuh -- the tile kernel with V adjacent lines per thread and 16-byte
+// vector accesses (HBM and shared memory), for the passes of large
+// transforms.
+//
+// The passes are those of tile.cuh (COL: C adjacent columns of a four-step
+// sub-problem, four-step twiddle on the way out; ROW: C adjacent rows, written
+// to their digit-reversed positions), and the arithmetic is the same radix-16
+// Stockham DIT steps in registers. What changes is the thread layout:
+//   - a thread owns V lines side by side (4 four-byte or 2 eight-byte values,
+//     16 bytes) and E points of each (16, or 8 for half the registers and
+//     more resident warps); its V independent E-point DFTs share one set of
+//     step-twiddle loads and index arithmetic;
+//   - a column pass loads and stores 16 bytes per access (V adjacent columns
+//     of one row); a row pass stores 16 bytes per access (V adjacent rows at
+//     one output position) and loads V scalars;
+//   - shared memory holds the tile point-major, [point][C lines]: each access
+//     moves one thread's 16 bytes, and the 8 threads of a quarter-warp phase
+//     (8 line groups at one point) cover one contiguous 128-byte row, so no
+//     padding is needed for any Stockham stride;
+//   - the grid covers the lines exactly (the host only picks shapes where C
+//     divides the lines of a sub-problem), so no access is predicated.
+// Replaces, like tile.cuh, the reference's one-stage-per-launch global passes
+// (stNttGlobalRadix2_first/_rest, st_ntt_global_radix2.cuh:8-117), whose
+// loads and stores are one 4-byte element per access (:60-75, :95-100).
+#pragma once
+#include <cstdint>
+
+#include "tile.cuh"
+
+namespace stntt {
+
+// 16 bytes of V elements: load / store between memory and V registers.
+template <class T, int V>
+__device__ __forceinline__ void v16_load(T (&x)[V], const T *p) {
+    if constexpr (sizeof(T) == 4) {
+        static_assert(V == 4, "16 bytes of 4-byte values");
+        const uint4 q = *reinterpret_cast<const uint4 *>(p);
+        x[0] = q.x, x[1] = q.y, x[2] = q.z, x[3] = q.w;
+    } else {
+        static_assert(V == 2, "16 bytes of 8-byte values");
+        const ulonglong2 q = *reinterpret_cast<const ulonglong2 *>(p);
+        x[0] = q.x, x[1] = q.y;
+    }
+}
+template <class T, int V>
+__device__ __forceinline__ void v16_store(T *p, const T (&x)[V]) {
+    if constexpr (sizeof(T) == 4)
+        *reinterpret_cast<uint4 *>(p) = make_uint4(x[0], x[1], x[2], x[3]);
+    else
+        *reinterpret_cast<ulonglong2 *>(p) = make_ulonglong2(x[0], x[1]);
+}
+// read-only global variant (through the non-coherent path)
+template <class T, int V>
+__device__ __forceinline__ void v16_ldg(T (&x)[V], const T *p) {
+    if constexpr (sizeof(T) == 4) {
+        const uint4 q = __ldg(reinterpret_cast<const uint4 *>(p));
+        x[0] = q.x, x[1] = q.y, x[2] = q.z, x[3] = q.w;
+    } else {
+        const ulonglong2 q = __ldg(reinterpret_cast<const ulonglong2 *>(p));
+        x[0] = q.x, x[1] = q.y;
+    }
+}
+
+// V twiddle entries at p (consecutive, 16-byte aligned): u32 Shoup pairs are
+// 8 bytes each (two 16-byte loads for V = 4), Goldilocks entries 8 bytes.
+template <class F, int V>
+__device__ __forceinline__ void tw_load_v(typename F::TW (&w)[V], const typename F::TW *p) {
+    static_assert(sizeof(typename F::TW) == 8, "8-byte twiddle entries");
+    const uint4 *q = reinterpret_cast<const uint4 *>(p);
+#pragma unroll
+    for (int i = 0; i < V / 2; ++i) {
+        const uint4 a = __ldg(q + i);
+        const unsigned long long lo = ((unsigned long long)a.y << 32) | a.x;
+        const unsigned long long hi = ((unsigned long long)a.w << 32) | a.z;
+        memcpy(&w[2 * i], &lo, 8);
+        memcpy(&w[2 * i + 1], &hi, 8);
+    }
+}
+
+// Where a thread's lines start in HBM.
+template <class T, int V>
+struct VGeo {
+    const T *src[V];   // COL: src[0] = element 0 of the thread's first column; ROW: row v's element 0
+    T *dst;            // COL: element 0 of the first column; ROW: output slot of the first row
+    uint32_t istride;  // COL: column stride (elements)
+    uint32_t ostride;  // COL: column stride; ROW: n / L (the digit-reversed output spacing)
+    uint32_t col0;     // COL: the thread's first column within its sub-problem
+};
+
+template <class F, int V, bool COL, bool FULL4>
+__device__ __forceinline__ void vstore_last(const TileArgs<F> &a, const F &f, const VGeo<typename F::T, V> &geo,
+                                            uint32_t pos, typename F::T (&v)[V]) {
+    using TW = typename F::TW;
+    if constexpr (COL) {
+        if constexpr (FULL4) {
+            TW w[V];
+            tw_load_v<F, V>(w, a.tw4_full + (uint64_t)pos * geo.ostride + geo.col0);
+#pragma unroll
+            for (int i = 0; i < V; ++i)
+                v[i] = f.mul_tw(v[i], w[i]);
+        } else {
+#pragma unroll
+            for (int i = 0; i < V; ++i) {
+                const uint64_t e = (uint64_t)(geo.col0 + i) * pos;
+                const uint32_t lo = (uint32_t)(e & ((1ull << a.h) - 1));
+                const uint32_t hi = (uint32_t)(e >> a.h);
+                v[i] = f.mul_tw(f.mul_tw(v[i], __ldg(&a.tw4_lo[lo])), __ldg(&a.tw4_hi[hi]));
+            }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < V; ++i)
+        v[i] = f.canon(v[i]);
+    v16_store<typename F::T, V>(geo.dst + (uint64_t)pos * geo.ostride, v);
+}
+
+// One radix-2^LOGR Stockham step over the tile (see tile_step_l): read R
+// points per item (HBM on the first step, else shared memory), twiddle,
+// R-point DFT per line, write R points (shared memory, or HBM on the last).
+template <class F, int V, int E, int LOGL, int LOGG, int LOGR, int LOGP, bool first, bool last, bool COL, bool FULL4>
+__device__ __forceinline__ void vstep(const TileArgs<F> &a, const F &f, typename F::T (&x)[V][E],
+                                      typename F::T *sm_g, uint32_t u, const VGeo<typename F::T, V> &geo) {
+    using T = typename F::T;
+    constexpr int R = 1 << LOGR, ITEMS = E / R;
+    constexpr uint32_t U = (1u << LOGL) / E, TS = (1u << LOGL) >> LOGR, P = 1u << LOGP, C = V << LOGG;
+    static_assert(LOGR + LOGP <= LOGL, "step beyond the tile");
+    if constexpr (last)
+        pdl_trigger();
+    // ---- read R points per item: idx = u + m U + r L/R
+#pragma unroll
+    for (int m = 0; m < ITEMS; ++m) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const uint32_t idx = u + m * U + r * TS;
+            T t[V];
+            if constexpr (first) {
+                if constexpr (COL) {
+                    v16_ldg<T, V>(t, geo.src[0] + (uint64_t)idx * geo.istride);
+                } else {
+#pragma unroll
+                    for (int i = 0; i < V; ++i)
+                        t[i] = __ldg(geo.src[i] + idx);
+                }
+            } else {
+                v16_load<T, V>(t, sm_g + idx * C);
+            }
+#pragma unroll
+            for (int i = 0; i < V; ++i)
+                x[i][m * R + r] = t[i];
+        }
+    }
+    // ---- twiddle w_(R p)^(r k), k = t mod p (shared by the V lines), then the DFTs
+#pragma unroll
+    for (int m = 0; m < ITEMS; ++m) {
+        if constexpr (!first) {
+            const uint32_t k = (u + m * U) & (P - 1);
+#pragma unroll
+            for (int r = 1; r < R; ++r) {
+                const typename F::TW w = __ldg(&a.twL[(r * k) << (LOGL - LOGR - LOGP)]);
+#pragma unroll
+                for (int i = 0; i < V; ++i)
+                    x[i][m * R + r] = f.mul_tw(x[i][m * R + r], w);
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < V; ++i)
+            dft_reg<F, R>(f, &x[i][m * R], a.wR);
+    }
+    if constexpr (!first && !last)
+        __syncthreads();  // every read of this step precedes any write
+    // ---- write output r of item t to (t - k) R + k + r p
+#pragma unroll
+    for (int m = 0; m < ITEMS; ++m) {
+        const uint32_t t = u + m * U;
+        const uint32_t k = t & (P - 1);
+        const uint32_t base = ((t - k) << LOGR) + k;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const uint32_t pos = base + ((uint32_t)r << LOGP);
+            T v[V];
+#pragma unroll
+            for (int i = 0; i < V; ++i)
+                v[i] = x[i][m * R + bit_reverse<LOGR>(r)];
+            if constexpr (last)
+                vstore_last<F, V, COL, FULL4>(a, f, geo, pos, v);
+            else
+                v16_store<T, V>(sm_g + pos * C, v);
+        }
+    }
+    if constexpr (!last)
+        __syncthreads();
+}
+
+// Steps S.. of the tile: one leading radix-2^(LOGL mod log2 E) step when
+// needed, then radix-E steps (E = 16, or 8 for half the registers).
+template <class F, int V, int E, int LOGL, int LOGG, int S, bool COL, bool FULL4>
+__device__ __forceinline__ void vsteps(const TileArgs<F> &a, const F &f, typename F::T (&x)[V][E],
+                                       typename F::T *sm_g, uint32_t u, const VGeo<typename F::T, V> &geo) {
+    static_assert(E == 8 || E == 16, "radix-8 or radix-16 steps");
+    constexpr int LE = E == 8 ? 3 : 4;
+    constexpr int TAIL = LOGL % LE;
+    constexpr int NS = LOGL / LE + (TAIL > 0 ? 1 : 0);
+    if constexpr (S < NS) {
+        constexpr int LOGR = (S == 0 && TAIL > 0) ? TAIL : LE;
+        constexpr int LOGP = S == 0 ? 0 : (TAIL > 0 ? TAIL + LE * (S - 1) : LE * S);
+        vstep<F, V, E, LOGL, LOGG, LOGR, LOGP, S == 0, S == NS - 1, COL, FULL4>(a, f, x, sm_g, u, geo);
+        vsteps<F, V, E, LOGL, LOGG, S + 1, COL, FULL4>(a, f, x, sm_g, u, geo);
+    }
+}
+
+// C = V * 2^LOGG lines per CTA, 2^LOGG * L/E threads (line group fastest).
+// Requirements the host checks: every pointer 16-byte aligned, C divides the
+// columns of a sub-problem (COL) or the rows of a transform (ROW), a
+// multi-pass plan (no n^-1 scaling in a row pass), no fused pointwise input.
+// Registers are capped per thread (the compiler otherwise keeps every
+// four-step twiddle of the last step live at once, up to 220 registers for
+// the 32-bit column passes at E = 16, and two CTAs of 128 threads fill an
+// SM). Measured on GB300 (32-bit 2^26, Goldilocks 2^24, forward + inverse):
+// E = 16: 128 registers (1.09 ms against 1.30 at 160 and 1.30 at 255);
+// E = 8: 64 for 4-byte values (1.03 ms against 1.20 at 80), 80 for 8-byte
+// ones (0.677 ms against 0.682 at 64).
+template <int E, int W>
+constexpr uint32_t vregs() {
+    return E == 16 ? 128 : (W == 8 ? 80 : 64);
+}
+template <int E, int W, uint32_t THREADS>
+constexpr uint32_t vminb() {
+    return (65536 / vregs<E, W>()) / THREADS > 0 ? (65536 / vregs<E, W>()) / THREADS : 1;
+}
+
+template <class F, int V, int E, int LOGL, int LOGG, bool COL, bool FULL4>
+__global__ void __launch_bounds__((1u << LOGG) * ((1u << LOGL) / E),
+                                  vminb<E, (int)sizeof(typename F::T), (1u << LOGG) * ((1u << LOGL) / E)>())
+    tile_kernel_v(const TileArgs<F> a) {
+    using T = typename F::T;
+    static_assert(LOGL >= 5, "at least two steps");
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr uint32_t G = 1u << LOGG, C = V * G;
+    const uint32_t g = threadIdx.x & (G - 1), u = threadIdx.x >> LOGG;
+    F f;
+    f.p = a.p;
+    const uint64_t line0 = (uint64_t)blockIdx.x * C + g * V;  // the thread's first line over the batch
+    const uint32_t logPer = a.logN - LOGL;                     // lines per transform
+    const uint64_t b = line0 >> logPer;
+    const uint64_t rem = line0 & ((1ull << logPer) - 1);
+    const T *ibase = a.in + (b << a.logN);
+    T *obase = a.out + (b << a.logN);
+    VGeo<T, V> geo;
+    if constexpr (COL) {
+        const uint64_t q = rem >> a.logS;
+        geo.col0 = (uint32_t)(rem & ((1ull << a.logS) - 1));
+        geo.src[0] = ibase + (q << a.logM) + geo.col0;
+#pragma unroll
+        for (int i = 1; i < V; ++i)
+            geo.src[i] = geo.src[0];
+        geo.dst = obase + (q << a.logM) + geo.col0;
+        geo.istride = geo.ostride = 1u << a.logS;
+    } else {
+#pragma unroll
+        for (int i = 0; i < V; ++i) {
+            const uint64_t r = rem + i;
+            const uint64_t inrow = ((r & ((1ull << a.logN1) - 1)) << a.logN2) + (r >> a.logN1);
+            geo.src[i] = ibase + (inrow << LOGL);
+        }
+        geo.dst = obase + rem;
+        geo.istride = 1;
+        geo.ostride = 1u << logPer;
+        geo.col0 = 0;
+    }
+    pdl_enter();
+    T x[V][E];
+    vsteps<F, V, E, LOGL, LOGG, 0, COL, FULL4>(a, f, x, reinterpret_cast<T *>(smem_raw) + g * V, u, geo);
+}
+
+}  // namespace stntt

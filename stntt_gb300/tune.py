@@ -45,11 +45,31 @@ def splits(log_n: int, max_pass: int = 13) -> list[list[int]]:
     return out
 
 
-def candidates(field: int, log_n: int, full: bool = False) -> Iterable[tuple[list[int], list[int], list[int]]]:
+def vec_candidates(field: int, logs: list[int]) -> Iterable[tuple[list[int], list[int], list[int]]]:
+    """The vector-lines build (STNTT_PASS_VEC) of a multi-pass split whose
+    passes are 2^7..2^10 points: 8 or 16 points per line per pass, 4 or 8
+    line groups per CTA (V = 4 lines per thread for the 32-bit field, 2 for
+    Goldilocks)."""
+    if len(logs) < 2 or not all(7 <= lg <= 10 for lg in logs):
+        return
+    v = 2 if field == st.FIELD_GL64 else 4
+    for es in itertools.product((8 | st.PASS_VEC, 16 | st.PASS_VEC), repeat=len(logs)):
+        for g in (4, 8):
+            yield list(logs), list(es), [g * v] * len(logs)
+
+
+def candidates(field: int, log_n: int, full: bool = False,
+               vec: bool = False) -> Iterable[tuple[list[int], list[int], list[int]]]:
     """Plan shapes to try: every columns-per-CTA choice, 16 or 32 elements per
     thread (and 8 where every pass is 2^7..2^11 points); without `full`, only
-    the three most even two-pass splits and the most even three-pass split."""
+    the three most even two-pass splits and the most even three-pass split;
+    with `vec`, also the vector-lines build of every three-pass split of
+    2^7..2^10-point passes."""
     sp = splits(log_n)
+    if vec:
+        for logs in sp:
+            if len(logs) == 3:
+                yield from vec_candidates(field, logs)
     if not full:
         two = sorted([s for s in sp if len(s) <= 2], key=lambda s: max(s) - min(s))[:3]
         three = sorted([s for s in sp if len(s) == 3], key=lambda s: max(s) - min(s))[:1]
@@ -93,7 +113,7 @@ def _time_plan(ctx: st.Context, field: int, log_n: int, data, p: int, root: int,
 
 
 def tune(ctx: st.Context, field: int, log_n: int, reps: int = 10, full: bool = False, verbose: bool = False,
-         batch: int = 0):
+         batch: int = 0, vec: bool = False):
     """Return (best_spec, best_us, all_results) for one size; leaves the best plan set.
     batch 0: enough transforms for 2^24 elements (a GPU-filling batch)."""
     import torch
@@ -111,7 +131,7 @@ def tune(ctx: st.Context, field: int, log_n: int, reps: int = 10, full: bool = F
         st.fill_uniform_u32(data, 99, p)
     flush = torch.empty(64 << 20, dtype=torch.int32, device=f"cuda:{ctx.device}")  # 256 MiB, twice L2
     results = []
-    for logs, es, cs in candidates(field, log_n, full):
+    for logs, es, cs in candidates(field, log_n, full, vec):
         try:
             ctx.set_plan(field, log_n, logs, es, cs, small=small)
             us = _time_plan(ctx, field, log_n, data, p, root, batch, reps, flush)
@@ -279,6 +299,7 @@ def main() -> None:
     ap.add_argument("--package", action="store_true", help="fold the results into the packaged plans")
     ap.add_argument("--batched", action="store_true",
                     help="tune the pass split of jobs in the persistent batched launch instead")
+    ap.add_argument("--vec", action="store_true", help="also try the vector-lines build of three-pass splits")
     args = ap.parse_args()
     field = st.FIELD_GL64 if args.field == "gl64" else st.FIELD_U32
     ctx = st.Context(0)
@@ -290,7 +311,7 @@ def main() -> None:
             allres[f"{args.field}:{lg}:batch"] = res
             print(json.dumps({"size": f"{args.field}:{lg}:batch", "best": best, "candidates": len(res)}), flush=True)
             continue
-        best, res = tune(ctx, field, lg, args.reps, args.full, args.verbose, args.batch)
+        best, res = tune(ctx, field, lg, args.reps, args.full, args.verbose, args.batch, args.vec)
         record(ctx, field, lg, best, Path(args.cache))
         allres[f"{args.field}:{lg}" + (":b1" if (best["batch"] << lg) < (1 << 22) else "")] = res
         print(json.dumps({"size": f"{args.field}:{lg}", "best": best, "candidates": len(res)}), flush=True)

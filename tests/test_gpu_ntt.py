@@ -625,7 +625,7 @@ def test_cluster_path_eight_elements(ctx, field, lg, logs):
 def test_stream_workspaces_release_and_cap(ctx):
     """Per-stream scratch: stntt_release_stream frees a stream's buffer, and a
     context keeps at most 64 of them (least recently used freed first)."""
-    lg = 14  # two HBM passes: a 2^14 * 8-byte workspace per stream
+    lg = 18  # two HBM passes (no one-launch cluster at this size): a 2^18 * 8-byte workspace per stream
     ws = (1 << lg) * 8
     x = O.uniform_u64(3, 1 << lg)
     want = O.ntt_gl64(x)
@@ -663,3 +663,150 @@ def test_host_call_reports_kernel_time(ctx):
     y = O.uniform_u64(5, 1 << 20)
     ctx.ntt_gl64_host(y, 20)
     assert ctx.last_kernel_ms() > 0.0
+
+
+VEC = st.PASS_VEC
+
+
+@pytest.mark.parametrize("field,lg,logs,batch,cols", [
+    ("gl64", 16, [8, 8], 64, 16),      # column pass with a full four-step table, row pass; 8 line groups
+    ("gl64", 22, [7, 7, 8], 1, 8),     # two-level four-step twiddle, full table, row; 4 line groups
+    ("gl64", 20, [10, 10], 4, 16),
+    ("gl64", 18, [9, 9], 16, 8),
+    ("u32", 16, [8, 8], 64, 32),
+    ("u32", 22, [7, 7, 8], 1, 16),
+    ("u32", 20, [10, 10], 4, 32),
+    ("u32", 18, [9, 9], 16, 16),
+])
+def test_vector_lines_build(ctx, field, lg, logs, batch, cols):
+    """STNTT_PASS_VEC: every pass in the vector-lines build (V adjacent lines
+    per thread, 16-byte accesses), forward and inverse, against the oracle;
+    an unaligned output falls back to the plain build with the same result."""
+    fid = st.FIELD_GL64 if field == "gl64" else st.FIELD_U32
+    k = len(logs)
+    try:
+        ctx.set_plan(fid, lg, logs, elems=[16 | VEC] * k, cols=[cols] * k)
+        n = 1 << lg
+        if field == "gl64":
+            x = O.uniform_u64(900 + lg, batch * n)
+            for inv in (False, True):
+                d = dev64(x)
+                ctx.ntt_gl64(d, lg, batch, inverse=inv)
+                assert np.array_equal(host64(d), O.ntt_gl64(x, inverse=inv, batch=batch, threads=8)), inv
+            src = dev64(x)
+            big = torch.zeros(batch * n + 1, dtype=torch.int64, device="cuda")
+            ctx.ntt_gl64_oop(src, big[1:], lg, batch)
+            assert np.array_equal(host64(big[1:]), O.ntt_gl64(x, batch=batch, threads=8))
+        else:
+            p, root = st.params_u32(lg)
+            x = O.uniform_u32(900 + lg, p, batch * n)
+            for inv in (False, True):
+                d = dev32(x)
+                ctx.ntt_u32(d, lg, batch, p, root, inverse=inv)
+                assert np.array_equal(host32(d), O.ntt_u32(x, root, p, inverse=inv, batch=batch, threads=8)), inv
+            src = dev32(x)
+            big = torch.zeros(batch * n + 1, dtype=torch.int32, device="cuda")
+            ctx.ntt_u32_oop(src, big[1:], lg, batch, p, root)
+            assert np.array_equal(host32(big[1:]), O.ntt_u32(x, root, p, batch=batch, threads=8))
+    finally:
+        ctx.clear_plans()
+        from stntt_gb300 import tune
+        tune.apply_cache(ctx)
+
+
+@pytest.mark.parametrize("field,lg,logs,cols", [("gl64", 24, [8, 8, 8], 16), ("u32", 26, [8, 9, 9], 32),
+                                                ("gl64", 24, [8, 8, 8], 8), ("u32", 26, [8, 9, 9], 16)])
+def test_vector_lines_build_full_size(ctx, field, lg, logs, cols):
+    """The large transforms in the vector-lines build equal the plain build
+    (which the oracle pins at these sizes) bit for bit, both directions."""
+    fid = st.FIELD_GL64 if field == "gl64" else st.FIELD_U32
+    n = 1 << lg
+    p, root = (0, 0) if field == "gl64" else st.params_u32(lg)
+    if field == "gl64":
+        x = torch.empty(n, dtype=torch.int64, device="cuda")
+        st.fill_uniform_gl64(x, 5)
+        run = lambda t, inv: ctx.ntt_gl64(t, lg, 1, inverse=inv)  # noqa: E731
+    else:
+        x = torch.empty(n, dtype=torch.int32, device="cuda")
+        st.fill_uniform_u32(x, 5, p)
+        run = lambda t, inv: ctx.ntt_u32(t, lg, 1, p, root, inverse=inv)  # noqa: E731
+    try:
+        want = {}
+        ctx.set_plan(fid, lg, logs)
+        for inv in (False, True):
+            t = x.clone()
+            run(t, inv)
+            want[inv] = t
+        ctx.set_plan(fid, lg, logs, elems=[16 | VEC] * 3, cols=[cols] * 3)
+        for inv in (False, True):
+            t = x.clone()
+            run(t, inv)
+            torch.cuda.synchronize()
+            assert torch.equal(t, want[inv]), inv
+    finally:
+        ctx.clear_plans()
+        from stntt_gb300 import tune
+        tune.apply_cache(ctx)
+
+
+@pytest.mark.parametrize("field,lg", [("gl64", 18), ("gl64", 19), ("gl64", 20), ("gl64", 21),
+                                      ("u32", 18), ("u32", 19), ("u32", 20), ("u32", 21)])
+def test_cooperative_two_pass_launch(ctx, field, lg):
+    """stntt_set_coop(1): single calls of 2^18..2^21 points run both passes in
+    one cooperative launch (grid-wide barrier): one launch per call,
+    bit-exact against the oracle in both directions, again after many calls
+    on one stream (the barrier words are reused), on a second stream, inside
+    a replayed CUDA graph, and equal to the two-launch path (the default)."""
+    fid = st.FIELD_GL64 if field == "gl64" else st.FIELD_U32
+    p, root = (0, 0) if field == "gl64" else st.params_u32(lg)
+    ctx.set_plan(fid, lg, [lg // 2, lg - lg // 2], elems=[8, 8], small=True)
+    ctx.set_coop(1)
+    launches, _ = ctx.call_info(fid, lg, 1, p, root)
+    assert launches == 1
+    n = 1 << lg
+    if field == "gl64":
+        x = O.uniform_u64(40 + lg, n)
+        want = {False: O.ntt_gl64(x), True: O.ntt_gl64(x, inverse=True)}
+        mk, get = dev64, host64
+        run = lambda t, inv, s=None: ctx.ntt_gl64(t, lg, 1, inverse=inv, stream=s)  # noqa: E731
+    else:
+        x = O.uniform_u32(40 + lg, p, n)
+        want = {False: O.ntt_u32(x, root, p), True: O.ntt_u32(x, root, p, inverse=True)}
+        mk, get = dev32, host32
+        run = lambda t, inv, s=None: ctx.ntt_u32(t, lg, 1, p, root, inverse=inv, stream=s)  # noqa: E731
+    for inv in (False, True):
+        d = mk(x)
+        run(d, inv)
+        assert np.array_equal(get(d), want[inv]), inv
+    d = mk(x)
+    for _ in range(25):  # forward + inverse, many barrier generations on one stream
+        run(d, False)
+        run(d, True)
+    assert np.array_equal(get(d), x)
+    s2 = torch.cuda.Stream()
+    d2 = mk(x)
+    run(d2, False, s2)
+    s2.synchronize()
+    assert np.array_equal(get(d2), want[False])
+    g = torch.cuda.CUDAGraph()
+    d3 = mk(x)
+    with torch.cuda.graph(g, stream=s2):
+        run(d3, False, s2)
+    for _ in range(2):
+        d3.copy_(mk(x))
+        torch.cuda.synchronize()
+        g.replay()
+        torch.cuda.synchronize()
+        assert np.array_equal(get(d3), want[False])
+    assert ctx.device_status() == 0
+    try:
+        ctx.set_coop(0)  # the default: two launches
+        assert ctx.call_info(fid, lg, 1, p, root)[0] == 2
+        d4 = mk(x)
+        run(d4, False)
+        assert np.array_equal(get(d4), want[False])
+    finally:
+        ctx.set_coop(0)
+        ctx.clear_plans()
+        from stntt_gb300 import tune
+        tune.apply_cache(ctx)
