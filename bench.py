@@ -603,6 +603,35 @@ def run_batch_mix(args):
 SERVE_RATE, SERVE_LO, SERVE_HI, SERVE_SEED = 20000.0, 12, 22, 0x57170001 + 4
 
 
+def device_stalls(torch, seconds: float = 1.5, threshold_ms: float = 2.0):
+    """How often this GPU stops for a while on its own: back-to-back tiny
+    kernels (no library code) on one stream for `seconds`, a CUDA event after
+    each; every gap between consecutive completions above threshold_ms is a
+    stall that any request in flight at that moment waits out. Reported beside
+    the serving latencies, whose tail such stalls set."""
+    s = torch.cuda.Stream()
+    x = torch.zeros(1024, dtype=torch.int32, device="cuda")
+    start = torch.cuda.Event(enable_timing=True)
+    evs = []
+    with torch.cuda.stream(s):
+        start.record(s)
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < seconds and len(evs) < 400000:
+            for _ in range(32):
+                x.add_(1)
+                e = torch.cuda.Event(enable_timing=True)
+                e.record(s)
+                evs.append(e)
+            if len(evs) % 1024 == 0:
+                evs[-1].synchronize()  # keep the device queue short: completions follow submissions
+    s.synchronize()
+    t = [start.elapsed_time(e) for e in evs]
+    gaps = [{"at_ms": round(t[i - 1], 2), "gap_ms": round(t[i] - t[i - 1], 2)}
+            for i in range(1, len(t)) if t[i] - t[i - 1] > threshold_ms]
+    return {"span_ms": round(t[-1], 1) if t else 0.0, "kernels": len(t), "threshold_ms": threshold_ms,
+            "stalls": gaps}
+
+
 def measure_serve(st, torch, local: int, count: int, streams: int, rate: float = SERVE_RATE):
     """Seeded Poisson stream (mean 20k requests/s): 70% single NTTs, 30%
     cyclic polynomial products of two polynomials of degree < n/2, n = 2^k with
@@ -645,6 +674,7 @@ def measure_serve(st, torch, local: int, count: int, streams: int, rate: float =
                                    a.data_ptr(), 0, o.data_ptr()))
     # warm-up: the first few requests, run to completion
     sv.run_trace(reqs[: min(200, count)], [0.0] * min(200, count))
+    stalls = device_stalls(torch)
     t0 = time.perf_counter()
     comps = sv.run_trace(reqs, list(arrivals))
     wall = time.perf_counter() - t0
@@ -662,7 +692,7 @@ def measure_serve(st, torch, local: int, count: int, streams: int, rate: float =
                        "queue_p50": float(np.percentile(qwait, 50)), "queue_p99": float(np.percentile(qwait, 99))},
         "throughput": {"requests_per_s": count / span, "offered_per_s": rate,
                        "transform_gelem_per_s": elems / span / 1e9, "span_s": span, "wall_s": wall},
-        "requests": count, "server": stats, "status_ok": ok}
+        "requests": count, "server": stats, "status_ok": ok, "device_stalls_before_trace": stalls}
 
 
 def run_serve_mix(args):
@@ -687,7 +717,7 @@ def run_serve_mix(args):
                        "log_n_range": [SERVE_LO, SERVE_HI], "polymul_fraction": 0.3, "fields": "50/50",
                        "streams": args.streams, "seed": SERVE_SEED},
             "latency_ms": m["latency_ms"], "throughput": m["throughput"], "server": m["server"], "clocks": clocks,
-            "status_ok": m["status_ok"]}), flush=True)
+            "status_ok": m["status_ok"], "device_stalls_before_trace": m["device_stalls_before_trace"]}), flush=True)
 
 
 # --------------------------------------------------------------------------- our arm, single transforms
@@ -810,7 +840,8 @@ def main():
         sv = measure_serve(st, torch, local, args.serve_requests or 20000, args.streams)
         secondary["serve_mix"] = {"latency_ms": sv["latency_ms"], "throughput": sv["throughput"],
                                   "requests": sv["requests"], "status_ok": sv["status_ok"],
-                                  "rate_per_s": SERVE_RATE, "log_n_range": [SERVE_LO, SERVE_HI]}
+                                  "rate_per_s": SERVE_RATE, "log_n_range": [SERVE_LO, SERVE_HI],
+                                  "device_stalls_before_trace": sv["device_stalls_before_trace"]}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -436,6 +437,19 @@ uint32_t tma_builtin(int field, const PassDesc &d) {
     return 0;
 }
 
+// Largest column-pass sub-problem (log2 points) of a plain-build pass of a
+// call of 2^22+ elements that reads its four-step twiddle from a full table:
+// kFullTwiddleMaxLog, or STNTT_FULL_TWIDDLE_MAX_LOG from the environment
+// (14..26; read once).
+uint32_t full_twiddle_max_log() {
+    static const uint32_t v = [] {
+        const char *e = getenv("STNTT_FULL_TWIDDLE_MAX_LOG");
+        const long x = e ? strtol(e, nullptr, 10) : -1;
+        return (x >= (long)kFullTwiddleMinLog && x <= 26) ? (uint32_t)x : kFullTwiddleMaxLog;
+    }();
+    return v;
+}
+
 // Build the pass list and the twiddle tables for one transform.
 int build_plan(stntt_ctx *ctx, Plan &pl, int field, uint32_t log_n, uint32_t p, uint64_t root_dir, int dir,
                const PlanSpec *spec, bool small_call) {
@@ -513,13 +527,6 @@ int build_plan(stntt_ctx *ctx, Plan &pl, int field, uint32_t log_n, uint32_t p, 
             const uint64_t wM = fpow(field, root_dir, n >> d.logM, p);
             d.lo_off = add_table(1ull << d.h, wM, 1);
             d.hi_off = add_table(1ull << (d.logM - d.h), fpow(field, wM, 1ull << d.h, p), i == 0 ? ninv : 1);
-            // Column passes over 2^14..2^20-point sub-problems read the twiddle
-            // w_M^(col*pos) from a table laid out like the data: one load and
-            // one product per element instead of two lookups and two products
-            // (M entries per plan; the lo / hi tables stay for the kernels
-            // without this path).
-            if (d.logM >= kFullTwiddleMinLog && d.logM <= (small_call ? kFullTwiddleMaxLogSmall : kFullTwiddleMaxLog))
-                d.full_off = add_full(1ull << d.logM, d.lo_off, d.hi_off, d.h, d.logS);
             col_limit = 1ull << d.logS;
         } else {
             d.mode = kModeRow;
@@ -536,6 +543,20 @@ int build_plan(stntt_ctx *ctx, Plan &pl, int field, uint32_t log_n, uint32_t p, 
                 col_limit = std::min<uint64_t>(col_limit, 1ull << (log_n - d.logL));
             shape_pass_vec(d, field, col_limit, want_e & 0xffu, spec ? spec->cols[i] : 0);
         }
+        // Column passes over 2^14..2^20-point sub-problems read the twiddle
+        // w_M^(col*pos) from a table laid out like the data: one load and one
+        // product per element instead of two lookups and two products (M
+        // entries per plan; the lo / hi tables stay for the kernels without
+        // this path). Passes in the vector-lines build, whose table loads are
+        // 16 bytes wide, use it up to 2^26-point sub-problems: the table then
+        // streams from HBM beside the data and still wins (measured on GB300,
+        // forward + inverse: Goldilocks 2^24 0.669 -> 0.631 ms, 2^22 0.186 ->
+        // 0.176 ms, 32-bit 2^26 1.015 -> 0.994 ms), at n * 8 bytes of table per
+        // plan. STNTT_FULL_TWIDDLE_MAX_LOG (14..26) moves the limit of the
+        // other passes of calls of 2^22+ elements.
+        if (d.mode == kModeCol && d.logM >= kFullTwiddleMinLog &&
+            d.logM <= (small_call ? kFullTwiddleMaxLogSmall : d.vec ? kFullTwiddleMaxLogVec : full_twiddle_max_log()))
+            d.full_off = add_full(1ull << d.logM, d.lo_off, d.hi_off, d.h, d.logS);
         d.tma = ctx->tma_mode < 0 ? tma_builtin(field, d) : (uint32_t)ctx->tma_mode;
         pl.passes.push_back(d);
         done += d.logL;

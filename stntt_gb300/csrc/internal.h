@@ -19,6 +19,9 @@ enum : uint32_t { kModeCol = 0, kModeRow = 1 };  // tile pass kinds (tile.cuh)
 // (measured on GB300, Goldilocks 2^20 forward + inverse with L2 flushed
 // between steps: 84.5 us with the full table, 77.8 us without).
 constexpr uint32_t kFullTwiddleMinLog = 14, kFullTwiddleMaxLog = 20, kFullTwiddleMaxLogSmall = 17;
+// Passes in the vector-lines build (tile_v.cuh) of calls of 2^22+ elements
+// use full tables up to 2^26-point sub-problems (see build_plan).
+constexpr uint32_t kFullTwiddleMaxLogVec = 26;
 // One-launch transforms: 16-CTA clusters (non-portable size) where the device
 // schedules them, else 8; up to 2^(15 + log2 K) bytes per transform.
 constexpr uint32_t kClusterLogSmall = 3, kClusterLogLarge = 4;
