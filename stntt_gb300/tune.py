@@ -63,12 +63,12 @@ def candidates(field: int, log_n: int, full: bool = False,
     """Plan shapes to try: every columns-per-CTA choice, 16 or 32 elements per
     thread (and 8 where every pass is 2^7..2^11 points); without `full`, only
     the three most even two-pass splits and the most even three-pass split;
-    with `vec`, also the vector-lines build of every three-pass split of
-    2^7..2^10-point passes."""
+    with `vec`, also the vector-lines build of every two- or three-pass split
+    of 2^7..2^10-point passes."""
     sp = splits(log_n)
     if vec:
         for logs in sp:
-            if len(logs) == 3:
+            if len(logs) >= 2:
                 yield from vec_candidates(field, logs)
     if not full:
         two = sorted([s for s in sp if len(s) <= 2], key=lambda s: max(s) - min(s))[:3]

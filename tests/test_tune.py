@@ -83,15 +83,18 @@ def test_packaged_plans_parse():
 
 
 def test_plan_candidates_offer_vector_lines_build():
-    """--vec adds the vector-lines build (STNTT_PASS_VEC) of three-pass splits
-    with 2^7..2^10-point passes: 8 or 16 points per line, 4 or 8 line groups."""
+    """--vec adds the vector-lines build (STNTT_PASS_VEC) of two- and
+    three-pass splits with 2^7..2^10-point passes: 8 or 16 points per line, 4
+    or 8 line groups."""
     from stntt_gb300 import tune
 
     cands = list(tune.candidates(st.FIELD_U32, 26, vec=True))
     vec = [c for c in cands if any(e & st.PASS_VEC for e in c[1])]
     assert ([9, 9, 8], [8 | st.PASS_VEC, 8 | st.PASS_VEC, 16 | st.PASS_VEC], [32, 32, 32]) in vec
-    assert all(len(logs) == 3 and all(7 <= lg <= 10 for lg in logs) and cols[0] in (16, 32)
+    assert all(len(logs) in (2, 3) and all(7 <= lg <= 10 for lg in logs) and cols[0] in (16, 32)
                for logs, _, cols in vec)
+    assert any(len(logs) == 2 for logs, es, _ in tune.candidates(st.FIELD_GL64, 20, vec=True)
+               if any(e & st.PASS_VEC for e in es))
     gl = [c for c in tune.candidates(st.FIELD_GL64, 24, vec=True) if any(e & st.PASS_VEC for e in c[1])]
     assert gl and all(cols[0] in (8, 16) for _, _, cols in gl)
     assert not any(e & st.PASS_VEC for c in tune.candidates(st.FIELD_GL64, 24) for e in c[1])
