@@ -157,6 +157,12 @@ cudaError_t launch_cluster(int field, const PassDesc &d1, const PassDesc &d2, ui
         return launch_cluster_u32l(d1, d2, p, tables, in, out, batch, xoff, xs, smem, log_k, s);
     return cudaErrorNotSupported;
 }
+cudaError_t gen_four_step_mont_u32(void *, const void *, const void *, uint32_t, uint32_t, uint64_t, uint32_t,
+                                   cudaStream_t);
+cudaError_t launch_gen_four_step_mont(void *out, const void *lo, const void *hi, uint32_t h, uint32_t logS,
+                                      uint64_t count, uint32_t p, cudaStream_t s) {
+    return gen_four_step_mont_u32(out, lo, hi, h, logS, count, p, s);
+}
 cudaError_t launch_gen_four_step(int field, void *out, const void *lo, const void *hi, uint32_t h, uint32_t logS,
                                  uint64_t count, uint32_t p, cudaStream_t s) {
     return field == kFieldGL ? gen_four_step_gl64(out, lo, hi, h, logS, count, p, s)
@@ -401,32 +407,39 @@ void shape_pass(PassDesc &d, int field, uint64_t col_limit, uint32_t want_E, uin
 
 // The vector-lines build of a pass (tile_v.cuh), when asked for (STNTT_PASS_VEC
 // in a plan's elements per thread) and the pass allows it: a pass of a
-// multi-pass plan with a tile of 2^7..2^10 points, E = 16 (or 8) points per
-// line per thread, V = 16 bytes / w lines per thread and C = V * 2^g lines per
-// CTA (g = 2 or 3), C dividing the pass's lines per sub-problem. want_C picks
-// C (0: 8 line groups where they fit, else 4).
+// multi-pass plan, E = 16 (or 8) points per line per thread, V = 16 bytes / w
+// lines per thread and C = V * 2^g lines per CTA, C dividing the pass's lines
+// per sub-problem. Tiles of 2^7..2^10 points take g = 3 or 2 (within 1024
+// threads), the wide tiles of two-pass plans (2^11 and 2^12 points) g = 2 or
+// 1 within 512 threads; 200 KiB of shared memory at most. want_C picks C (0:
+// the most line groups that fit).
+size_t vec_smem(uint32_t V, uint32_t logG, uint32_t logL, uint32_t w) {
+    const uint32_t pb = logG < 3 ? 3 - logG : 0;  // one 16-byte pad per 2^pb points (tile_v.cuh, vpoint)
+    return ((size_t)V << logG) * (1u << logL) * w + (pb ? (size_t)((1u << logL) >> pb) * 16 : 0);
+}
+
 void shape_pass_vec(PassDesc &d, int field, uint64_t col_limit, uint32_t want_E, uint32_t want_C) {
     d.vec = 0;
-    if (d.logL < 7 || d.logL > 10 || d.do_scale || d.logL >= d.logN)
+    if (d.logL < 7 || d.logL > 12 || d.do_scale || d.logL >= d.logN)
         return;
     const uint32_t V = field == kFieldGL ? 2 : 4, w = field == kFieldGL ? 8 : 4;
     d.vE = want_E == 8 ? 8 : 16;
     const uint32_t U = (1u << d.logL) / d.vE;
-    uint32_t logG = 3;
-    if (want_C >= 4 * V && want_C <= 8 * V)
-        logG = want_C >= 8 * V ? 3 : 2;
-    while (logG >= 2 && ((uint64_t)V << logG) > col_limit)
+    const uint32_t gmax = d.logL <= 10 ? 3 : 2, gmin = d.logL <= 10 ? 2 : 1;
+    const uint32_t tmax = d.logL <= 10 ? 1024 : 512;
+    uint32_t logG = gmax;
+    for (uint32_t g = gmin; g <= gmax; ++g)
+        if (want_C == (V << g))
+            logG = g;
+    while (logG > gmin && (((uint64_t)V << logG) > col_limit || vec_smem(V, logG, d.logL, w) > 200 * 1024 ||
+                           (U << logG) > tmax))
         --logG;
-    while (logG > 2 && (((size_t)V << logG) * (1u << d.logL) * w > 200 * 1024 || (U << logG) > 1024))
-        --logG;
-    if (logG < 2 || ((uint64_t)V << logG) > col_limit || (U << logG) > 1024)
+    if (((uint64_t)V << logG) > col_limit || (U << logG) > tmax || vec_smem(V, logG, d.logL, w) > 200 * 1024)
         return;
     d.vec = V;
     d.vlogG = logG;
     d.vthreads = U << logG;
-    d.vsmem = ((size_t)V << logG) * (1u << d.logL) * w;
-    if (d.vsmem > 200 * 1024)
-        d.vec = 0;
+    d.vsmem = vec_smem(V, logG, d.logL, w);
 }
 
 // Whether a pass runs TMA-staged (tma.cuh) by default; the kernel still
@@ -448,6 +461,14 @@ uint32_t full_twiddle_max_log() {
         return (x >= (long)kFullTwiddleMinLog && x <= 26) ? (uint32_t)x : kFullTwiddleMaxLog;
     }();
     return v;
+}
+
+// -p^-1 mod 2^32 for odd p (Newton's iteration doubles the correct low bits).
+uint32_t neg_inv32(uint32_t p) {
+    uint32_t x = p;  // p * p = 1 mod 8: three bits
+    for (int i = 0; i < 4; ++i)
+        x *= 2u - p * x;
+    return 0u - x;
 }
 
 // Build the pass list and the twiddle tables for one transform.
@@ -479,22 +500,23 @@ int build_plan(stntt_ctx *ctx, Plan &pl, int field, uint32_t log_n, uint32_t p, 
         bool full;
         uint64_t lo_off, hi_off;
         uint32_t h, logS;
+        bool mont;  // full table of 4-byte Montgomery entries (count = entries)
     };
     std::vector<TableReq> reqs;
     uint64_t off = 0;
     // every table starts on a 32-byte boundary (vector loads of 2 or 4 entries)
     auto add_table = [&](uint64_t count, uint64_t base, uint64_t scale) {
         off = (off + 3) & ~3ull;
-        reqs.push_back({off, count, base, scale, false, 0, 0, 0, 0});
+        reqs.push_back({off, count, base, scale, false, 0, 0, 0, 0, false});
         const uint64_t o = off;
         off += count;
         return o;
     };
-    auto add_full = [&](uint64_t count, uint64_t lo_off, uint64_t hi_off, uint32_t h, uint32_t logS) {
+    auto add_full = [&](uint64_t count, uint64_t lo_off, uint64_t hi_off, uint32_t h, uint32_t logS, bool mont) {
         off = (off + 3) & ~3ull;
-        reqs.push_back({off, count, 0, 0, true, lo_off, hi_off, h, logS});
+        reqs.push_back({off, count, 0, 0, true, lo_off, hi_off, h, logS, mont});
         const uint64_t o = off;
-        off += count;
+        off += mont ? (count + 1) / 2 : count;  // 4-byte Montgomery entries take half the 8-byte slots
         return o;
     };
     const uint64_t modulus = field == kFieldGL ? GL_P : p;
@@ -555,8 +577,15 @@ int build_plan(stntt_ctx *ctx, Plan &pl, int field, uint32_t log_n, uint32_t p, 
         // plan. STNTT_FULL_TWIDDLE_MAX_LOG (14..26) moves the limit of the
         // other passes of calls of 2^22+ elements.
         if (d.mode == kModeCol && d.logM >= kFullTwiddleMinLog &&
-            d.logM <= (small_call ? kFullTwiddleMaxLogSmall : d.vec ? kFullTwiddleMaxLogVec : full_twiddle_max_log()))
-            d.full_off = add_full(1ull << d.logM, d.lo_off, d.hi_off, d.h, d.logS);
+            d.logM <= (small_call ? kFullTwiddleMaxLogSmall : d.vec ? kFullTwiddleMaxLogVec : full_twiddle_max_log())) {
+            // Beyond 2^20 points the 32-bit table streams from HBM: there its
+            // entries are 4-byte Montgomery values instead of 8-byte Shoup
+            // pairs (a 2^26-point table: 256 MiB instead of 512 MiB to read
+            // beside the 256 MiB of data), at two more multiplies per product.
+            d.full_mont = (field != kFieldGL && d.vec && d.logM > kFullTwiddleMaxLog && p < (1u << 30)) ? 1 : 0;
+            d.pinv = d.full_mont ? neg_inv32(p) : 0;
+            d.full_off = add_full(1ull << d.logM, d.lo_off, d.hi_off, d.h, d.logS, d.full_mont != 0);
+        }
         d.tma = ctx->tma_mode < 0 ? tma_builtin(field, d) : (uint32_t)ctx->tma_mode;
         pl.passes.push_back(d);
         done += d.logL;
@@ -570,9 +599,11 @@ int build_plan(stntt_ctx *ctx, Plan &pl, int field, uint32_t log_n, uint32_t p, 
     }
     char *tb = static_cast<char *>(pl.d_tables);
     for (const auto &r : reqs) {
-        e = r.full ? launch_gen_four_step(field, tb + r.at * esz, tb + r.lo_off * esz, tb + r.hi_off * esz, r.h,
-                                          r.logS, r.count, p, ctx->setup)
-                   : launch_gen_powers(field, tb + r.at * esz, r.count, r.base, r.scale, p, ctx->setup);
+        e = r.mont   ? launch_gen_four_step_mont(tb + r.at * esz, tb + r.lo_off * esz, tb + r.hi_off * esz, r.h, r.logS,
+                                                 r.count, p, ctx->setup)
+            : r.full ? launch_gen_four_step(field, tb + r.at * esz, tb + r.lo_off * esz, tb + r.hi_off * esz, r.h,
+                                            r.logS, r.count, p, ctx->setup)
+                     : launch_gen_powers(field, tb + r.at * esz, r.count, r.base, r.scale, p, ctx->setup);
         if (e != cudaSuccess)
             return cuda_fail(ctx, e, "twiddle generation launch");
     }

@@ -67,6 +67,15 @@ struct FieldU32L {
     __device__ __forceinline__ T mul(T a, T b) const { return (uint32_t)(((uint64_t)a * b) % p); }
     __device__ __forceinline__ static T tw_value(TW w) { return w.x; }
     __device__ __forceinline__ T canon(T a) const { return min(a, a - p); }
+    // a * w for a table entry wr = w * 2^32 mod p (Montgomery form, 4 bytes
+    // instead of a Shoup pair's 8): REDC(a * wr) with pinv = -p^-1 mod 2^32.
+    // For a < 2p, wr < p: (a wr + m p) / 2^32 < 2p, so the result rests in
+    // [0, 2p) like every lazy value; lo + (m p mod 2^32) is 0 or 2^32.
+    __device__ __forceinline__ T mul_mont(T a, uint32_t wr, uint32_t pinv) const {
+        const uint32_t lo = a * wr, hi = __umulhi(a, wr);
+        const uint32_t m = lo * pinv;
+        return hi + __umulhi(m, p) + (lo != 0u);
+    }
 };
 
 struct FieldGL {

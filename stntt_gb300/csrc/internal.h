@@ -46,6 +46,10 @@ struct PassDesc {
     // (unaligned pointers, a prime of 2^30 or more).
     uint32_t vec = 0, vE = 16, vlogG = 0, vthreads = 0;
     size_t vsmem = 0;
+    // 32-bit vector-lines column pass: the table at full_off holds M 4-byte
+    // Montgomery entries (w * 2^32 mod p) instead of Shoup pairs; the plain
+    // build, which cannot read it, takes the two-level tables instead.
+    uint32_t full_mont = 0, pinv = 0;
 };
 
 // ---- launchers (return the CUDA error of the launch) ----------------------
@@ -84,6 +88,10 @@ cudaError_t launch_coop(int field, const PassDesc &d1, const PassDesc &d2, uint3
 // two-level tables lo (w_M^e, e < 2^h) and hi (s * w_M^(e 2^h)).
 cudaError_t launch_gen_four_step(int field, void *out, const void *lo, const void *hi, uint32_t h, uint32_t logS,
                                  uint64_t count, uint32_t p, cudaStream_t s);
+// The same table for the 32-bit field in Montgomery form: out (4-byte entries)
+// = w_M^(col * pos) * 2^32 mod p, from the Shoup-pair tables lo / hi.
+cudaError_t launch_gen_four_step_mont(void *out, const void *lo, const void *hi, uint32_t h, uint32_t logS,
+                                      uint64_t count, uint32_t p, cudaStream_t s);
 cudaError_t launch_pointwise(int field, const void *a, const void *b, void *out, size_t count, uint32_t p,
                              cudaStream_t s);
 cudaError_t launch_fill_uniform(int field, void *out, size_t count, uint64_t seed, uint32_t p, cudaStream_t s);

@@ -204,7 +204,9 @@ void fill_args(TileArgs<F> &a, const PassDesc &d, uint32_t p, const void *tables
     a.twL = tab + d.tw_off;
     a.tw4_lo = tab + d.lo_off;
     a.tw4_hi = tab + d.hi_off;
-    a.tw4_full = d.full_off == ~0ull ? nullptr : tab + d.full_off;
+    a.tw4_full = (d.full_off == ~0ull || d.full_mont) ? nullptr : tab + d.full_off;
+    a.tw4_mont = (d.full_off != ~0ull && d.full_mont) ? reinterpret_cast<const uint32_t *>(tab + d.full_off) : nullptr;
+    a.pinv = d.pinv;
     for (int j = 0; j < 8; ++j)
         std::memcpy(&a.wR[j], &d.wR[j], sizeof(TW));
     std::memcpy(&a.scale, &d.scale, sizeof(TW));

@@ -229,6 +229,9 @@ cudaError_t launch_find_params(uint64_t size, uint64_t min_mod, uint64_t *out, c
     return cudaGetLastError();
 }
 
+__global__ void gen_four_step_mont_kernel(uint32_t *out, const uint2 *lo, const uint2 *hi, uint32_t h, uint32_t logS,
+                                          uint64_t count, uint32_t p);
+
 cudaError_t preload_u32() {
     cudaFuncAttributes at;
     cudaError_t e = preload_tiles_t<FieldU32>();
@@ -244,7 +247,31 @@ cudaError_t preload_u32() {
         e = cudaFuncGetAttributes(&at, copy_scale_kernel<FieldU32>);
     if (e == cudaSuccess)
         e = cudaFuncGetAttributes(&at, fill_uniform_u32_kernel);
+    if (e == cudaSuccess)
+        e = cudaFuncGetAttributes(&at, gen_four_step_mont_kernel);
     return e;
+}
+
+// out[pos * S + col] = w_M^(col * pos) * 2^32 mod p (Montgomery form), e = col * pos < M
+__global__ void gen_four_step_mont_kernel(uint32_t *out, const uint2 *lo, const uint2 *hi, uint32_t h, uint32_t logS,
+                                          uint64_t count, uint32_t p) {
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count)
+        return;
+    const uint64_t e = (i >> logS) * (i & ((1ull << logS) - 1));
+    const uint64_t w = (uint64_t)lo[e & ((1ull << h) - 1)].x * hi[e >> h].x % p;
+    out[i] = (uint32_t)((w << 32) % p);
+}
+
+cudaError_t gen_four_step_mont_u32(void *out, const void *lo, const void *hi, uint32_t h, uint32_t logS, uint64_t count,
+                                   uint32_t p, cudaStream_t s) {
+    const uint64_t blocks = (count + 255) / 256;
+    if (!blocks)
+        return cudaSuccess;
+    gen_four_step_mont_kernel<<<(unsigned)blocks, 256, 0, s>>>(static_cast<uint32_t *>(out),
+                                                               static_cast<const uint2 *>(lo),
+                                                               static_cast<const uint2 *>(hi), h, logS, count, p);
+    return cudaGetLastError();
 }
 
 cudaError_t gen_four_step_u32(void *out, const void *lo, const void *hi, uint32_t h, uint32_t logS, uint64_t count,

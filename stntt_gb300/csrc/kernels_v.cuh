@@ -34,7 +34,7 @@ cudaError_t vattr() {
     return cudaSuccess;
 }
 
-template <class F, int E, int LOGL, int LOGG, bool COL, bool FULL4>
+template <class F, int E, int LOGL, int LOGG, bool COL, int FULL4>
 cudaError_t launch_v(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks, cudaStream_t s) {
     constexpr auto kern = tile_kernel_v<F, vlines<F>(), E, LOGL, LOGG, COL, FULL4>;
     cudaError_t e = vattr<F, kern>();
@@ -61,18 +61,39 @@ cudaError_t launch_v(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks, c
 template <class F, int E, int LOGL, int LOGG>
 cudaError_t launch_v_mode(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks, cudaStream_t s) {
     if (d.mode == kModeRow)
-        return launch_v<F, E, LOGL, LOGG, false, false>(d, a, blocks, s);
+        return launch_v<F, E, LOGL, LOGG, false, 0>(d, a, blocks, s);
+    if constexpr (sizeof(typename F::T) == 4) {
+        if (a.tw4_mont)
+            return launch_v<F, E, LOGL, LOGG, true, 2>(d, a, blocks, s);
+    }
     if (a.tw4_full)
-        return launch_v<F, E, LOGL, LOGG, true, true>(d, a, blocks, s);
-    return launch_v<F, E, LOGL, LOGG, true, false>(d, a, blocks, s);
+        return launch_v<F, E, LOGL, LOGG, true, 1>(d, a, blocks, s);
+    return launch_v<F, E, LOGL, LOGG, true, 0>(d, a, blocks, s);
 }
 
 template <class F, int E, int LOGL>
 cudaError_t launch_v_g(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks, cudaStream_t s) {
-    switch (d.vlogG) {
-    case 2: return launch_v_mode<F, E, LOGL, 2>(d, a, blocks, s);
-    case 3: return launch_v_mode<F, E, LOGL, 3>(d, a, blocks, s);
-    default: return cudaErrorNotSupported;
+    // line groups per CTA: 4 or 8 up to 2^10-point tiles; 1 or 2 for the wide
+    // tiles of two-pass plans (2^11 and 2^12 points), at most 512 threads (at
+    // 1024 the 64-register limit spills the tile)
+    if constexpr (LOGL <= 10) {
+        switch (d.vlogG) {
+        case 2: return launch_v_mode<F, E, LOGL, 2>(d, a, blocks, s);
+        case 3: return launch_v_mode<F, E, LOGL, 3>(d, a, blocks, s);
+        default: return cudaErrorNotSupported;
+        }
+    } else {
+        switch (d.vlogG) {
+        case 1:
+            if constexpr ((2u << LOGL) / E <= 512)
+                return launch_v_mode<F, E, LOGL, 1>(d, a, blocks, s);
+            return cudaErrorNotSupported;
+        case 2:
+            if constexpr ((4u << LOGL) / E <= 512)
+                return launch_v_mode<F, E, LOGL, 2>(d, a, blocks, s);
+            return cudaErrorNotSupported;
+        default: return cudaErrorNotSupported;
+        }
     }
 }
 
@@ -83,6 +104,8 @@ cudaError_t launch_v_l(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks,
     case 8: return launch_v_g<F, E, 8>(d, a, blocks, s);
     case 9: return launch_v_g<F, E, 9>(d, a, blocks, s);
     case 10: return launch_v_g<F, E, 10>(d, a, blocks, s);
+    case 11: return launch_v_g<F, E, 11>(d, a, blocks, s);
+    case 12: return launch_v_g<F, E, 12>(d, a, blocks, s);
     default: return cudaErrorNotSupported;
     }
 }
@@ -102,7 +125,7 @@ cudaError_t launch_tile_vec_t(const PassDesc &d, uint32_t p, const void *tables,
         return cudaErrorNotSupported;
     TileArgs<F> a;
     fill_args<F>(a, d, p, tables, in, out);
-    if (a.tw4_full && !aligned16(a.tw4_full))
+    if ((a.tw4_full && !aligned16(a.tw4_full)) || (a.tw4_mont && !aligned16(a.tw4_mont)))
         return cudaErrorNotSupported;
     a.total = batch << (d.logN - d.logL);
     const uint64_t blocks = a.total / C;
@@ -115,19 +138,32 @@ cudaError_t launch_tile_vec_t(const PassDesc &d, uint32_t p, const void *tables,
 
 template <class F, int E, int LOGL, int LOGG>
 cudaError_t preload_v_lg() {
-    cudaError_t e = vattr<F, tile_kernel_v<F, vlines<F>(), E, LOGL, LOGG, false, false>>();
+    cudaError_t e = vattr<F, tile_kernel_v<F, vlines<F>(), E, LOGL, LOGG, false, 0>>();
     if (e == cudaSuccess)
-        e = vattr<F, tile_kernel_v<F, vlines<F>(), E, LOGL, LOGG, true, false>>();
+        e = vattr<F, tile_kernel_v<F, vlines<F>(), E, LOGL, LOGG, true, 0>>();
     if (e == cudaSuccess)
-        e = vattr<F, tile_kernel_v<F, vlines<F>(), E, LOGL, LOGG, true, true>>();
+        e = vattr<F, tile_kernel_v<F, vlines<F>(), E, LOGL, LOGG, true, 1>>();
+    if constexpr (sizeof(typename F::T) == 4) {
+        if (e == cudaSuccess)
+            e = vattr<F, tile_kernel_v<F, vlines<F>(), E, LOGL, LOGG, true, 2>>();
+    }
     return e;
+}
+
+// the wide-tile shapes launch_v_g / launch_tile_vec_t can pick (else nothing to load)
+template <class F, int E, int LOGL, int LOGG>
+cudaError_t preload_v_wide() {
+    if constexpr (((1u << LOGG) << LOGL) / E <= 512)
+        return preload_v_lg<F, E, LOGL, LOGG>();
+    return cudaSuccess;
 }
 
 template <class F, int E>
 cudaError_t preload_v_e() {
     const cudaError_t list[] = {preload_v_lg<F, E, 7, 2>(),  preload_v_lg<F, E, 7, 3>(),  preload_v_lg<F, E, 8, 2>(),
                                 preload_v_lg<F, E, 8, 3>(),  preload_v_lg<F, E, 9, 2>(),  preload_v_lg<F, E, 9, 3>(),
-                                preload_v_lg<F, E, 10, 2>(), preload_v_lg<F, E, 10, 3>()};
+                                preload_v_lg<F, E, 10, 2>(), preload_v_lg<F, E, 10, 3>(), preload_v_wide<F, E, 11, 1>(),
+                                preload_v_wide<F, E, 11, 2>(), preload_v_wide<F, E, 12, 1>(), preload_v_wide<F, E, 12, 2>()};
     for (cudaError_t e : list)
         if (e != cudaSuccess)
             return e;

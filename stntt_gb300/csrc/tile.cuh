@@ -64,6 +64,11 @@ struct TileArgs {
     // Optional second input (pointwise product fused into the first step):
     // the pass transforms in[j] * in2[j] (same layout as in).
     const T *in2;
+    // COL, 32-bit field, vector-lines build only: the full four-step table in
+    // Montgomery form (4 bytes per entry, w * 2^32 mod p, at pos * S + col)
+    // and pinv = -p^-1 mod 2^32.
+    const uint32_t *tw4_mont;
+    uint32_t pinv;
 };
 
 template <class F>

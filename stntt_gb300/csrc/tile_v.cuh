@@ -14,9 +14,10 @@
 //     of one row); a row pass stores 16 bytes per access (V adjacent rows at
 //     one output position) and loads V scalars;
 //   - shared memory holds the tile point-major, [point][C lines]: each access
-//     moves one thread's 16 bytes, and the 8 threads of a quarter-warp phase
-//     (8 line groups at one point) cover one contiguous 128-byte row, so no
-//     padding is needed for any Stockham stride;
+//     moves one thread's 16 bytes; with 8 line groups the 8 threads of a
+//     quarter-warp phase cover one contiguous 128-byte row, so no padding is
+//     needed for any Stockham stride; with 1, 2 or 4 line groups a 16-byte
+//     pad after every 128 bytes of points keeps strided writes apart;
 //   - the grid covers the lines exactly (the host only picks shapes where C
 //     divides the lines of a sub-problem), so no access is predicated.
 // Replaces, like tile.cuh, the reference's one-stage-per-launch global passes
@@ -87,12 +88,21 @@ struct VGeo {
     uint32_t col0;     // COL: the thread's first column within its sub-problem
 };
 
-template <class F, int V, bool COL, bool FULL4>
+// FULL4: 0 two-level four-step lookup, 1 full table of twiddle entries,
+// 2 full table of 4-byte Montgomery entries (32-bit field).
+template <class F, int V, bool COL, int FULL4>
 __device__ __forceinline__ void vstore_last(const TileArgs<F> &a, const F &f, const VGeo<typename F::T, V> &geo,
                                             uint32_t pos, typename F::T (&v)[V]) {
     using TW = typename F::TW;
     if constexpr (COL) {
-        if constexpr (FULL4) {
+        if constexpr (FULL4 == 2) {
+            static_assert(V == 4, "Montgomery tables serve the 32-bit field");
+            const uint4 w = __ldg(reinterpret_cast<const uint4 *>(a.tw4_mont + (uint64_t)pos * geo.ostride + geo.col0));
+            v[0] = f.mul_mont(v[0], w.x, a.pinv);
+            v[1] = f.mul_mont(v[1], w.y, a.pinv);
+            v[2] = f.mul_mont(v[2], w.z, a.pinv);
+            v[3] = f.mul_mont(v[3], w.w, a.pinv);
+        } else if constexpr (FULL4 == 1) {
             TW w[V];
             tw_load_v<F, V>(w, a.tw4_full + (uint64_t)pos * geo.ostride + geo.col0);
 #pragma unroll
@@ -114,16 +124,29 @@ __device__ __forceinline__ void vstore_last(const TileArgs<F> &a, const F &f, co
     v16_store<typename F::T, V>(geo.dst + (uint64_t)pos * geo.ostride, v);
 }
 
+// Element offset of a point's C lines in the shared-memory tile. With 8 line
+// groups (128 bytes per point) points are packed. With fewer, a quarter-warp
+// phase (8 threads x 16 bytes) spans 8 / 2^LOGG points, and Stockham writes
+// of points R apart would land on the same banks; one 16-byte pad after every
+// 8 / 2^LOGG points shifts consecutive rows of 128 bytes by a bank quarter
+// (the scheme of the plain build's padding, at 16-byte granularity).
+template <int V, int LOGG>
+__device__ __forceinline__ constexpr uint32_t vpoint(uint32_t point) {
+    constexpr uint32_t C = V << LOGG, PB = LOGG < 3 ? 3 - LOGG : 0;
+    return PB ? point * C + (point >> PB) * V : point * C;
+}
+
 // One radix-2^LOGR Stockham step over the tile (see tile_step_l): read R
 // points per item (HBM on the first step, else shared memory), twiddle,
 // R-point DFT per line, write R points (shared memory, or HBM on the last).
-template <class F, int V, int E, int LOGL, int LOGG, int LOGR, int LOGP, bool first, bool last, bool COL, bool FULL4>
+template <class F, int V, int E, int LOGL, int LOGG, int LOGR, int LOGP, bool first, bool last, bool COL, int FULL4>
 __device__ __forceinline__ void vstep(const TileArgs<F> &a, const F &f, typename F::T (&x)[V][E],
                                       typename F::T *sm_g, uint32_t u, const VGeo<typename F::T, V> &geo) {
     using T = typename F::T;
     constexpr int R = 1 << LOGR, ITEMS = E / R;
     constexpr uint32_t U = (1u << LOGL) / E, TS = (1u << LOGL) >> LOGR, P = 1u << LOGP, C = V << LOGG;
     static_assert(LOGR + LOGP <= LOGL, "step beyond the tile");
+    const auto at = [](uint32_t point) { return vpoint<V, LOGG>(point); };
     if constexpr (last)
         pdl_trigger();
     // ---- read R points per item: idx = u + m U + r L/R
@@ -142,7 +165,7 @@ __device__ __forceinline__ void vstep(const TileArgs<F> &a, const F &f, typename
                         t[i] = __ldg(geo.src[i] + idx);
                 }
             } else {
-                v16_load<T, V>(t, sm_g + idx * C);
+                v16_load<T, V>(t, sm_g + at(idx));
             }
 #pragma unroll
             for (int i = 0; i < V; ++i)
@@ -184,7 +207,7 @@ __device__ __forceinline__ void vstep(const TileArgs<F> &a, const F &f, typename
             if constexpr (last)
                 vstore_last<F, V, COL, FULL4>(a, f, geo, pos, v);
             else
-                v16_store<T, V>(sm_g + pos * C, v);
+                v16_store<T, V>(sm_g + at(pos), v);
         }
     }
     if constexpr (!last)
@@ -193,7 +216,7 @@ __device__ __forceinline__ void vstep(const TileArgs<F> &a, const F &f, typename
 
 // Steps S.. of the tile: one leading radix-2^(LOGL mod log2 E) step when
 // needed, then radix-E steps (E = 16, or 8 for half the registers).
-template <class F, int V, int E, int LOGL, int LOGG, int S, bool COL, bool FULL4>
+template <class F, int V, int E, int LOGL, int LOGG, int S, bool COL, int FULL4>
 __device__ __forceinline__ void vsteps(const TileArgs<F> &a, const F &f, typename F::T (&x)[V][E],
                                        typename F::T *sm_g, uint32_t u, const VGeo<typename F::T, V> &geo) {
     static_assert(E == 8 || E == 16, "radix-8 or radix-16 steps");
@@ -228,7 +251,7 @@ constexpr uint32_t vminb() {
     return (65536 / vregs<E, W>()) / THREADS > 0 ? (65536 / vregs<E, W>()) / THREADS : 1;
 }
 
-template <class F, int V, int E, int LOGL, int LOGG, bool COL, bool FULL4>
+template <class F, int V, int E, int LOGL, int LOGG, bool COL, int FULL4>
 __global__ void __launch_bounds__((1u << LOGG) * ((1u << LOGL) / E),
                                   vminb<E, (int)sizeof(typename F::T), (1u << LOGG) * ((1u << LOGL) / E)>())
     tile_kernel_v(const TileArgs<F> a) {

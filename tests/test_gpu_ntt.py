@@ -677,6 +677,10 @@ VEC = st.PASS_VEC
     ("u32", 22, [7, 7, 8], 1, 16),
     ("u32", 20, [10, 10], 4, 32),
     ("u32", 18, [9, 9], 16, 16),
+    ("gl64", 22, [11, 11], 1, 4),      # wide two-pass tiles, 2 line groups (padded shared memory)
+    ("gl64", 23, [11, 12], 1, 4),
+    ("u32", 22, [11, 11], 1, 16),      # 4 line groups of 2^11 points
+    ("u32", 23, [12, 11], 1, 8),
 ])
 def test_vector_lines_build(ctx, field, lg, logs, batch, cols):
     """STNTT_PASS_VEC: every pass in the vector-lines build (V adjacent lines
@@ -715,7 +719,8 @@ def test_vector_lines_build(ctx, field, lg, logs, batch, cols):
 
 
 @pytest.mark.parametrize("field,lg,logs,cols", [("gl64", 24, [8, 8, 8], 16), ("u32", 26, [8, 9, 9], 32),
-                                                ("gl64", 24, [8, 8, 8], 8), ("u32", 26, [8, 9, 9], 16)])
+                                                ("gl64", 24, [8, 8, 8], 8), ("u32", 26, [8, 9, 9], 16),
+                                                ("gl64", 24, [12, 12], 4), ("u32", 24, [12, 12], 8)])
 def test_vector_lines_build_full_size(ctx, field, lg, logs, cols):
     """The large transforms in the vector-lines build equal the plain build
     (which the oracle pins at these sizes) bit for bit, both directions."""
@@ -737,7 +742,7 @@ def test_vector_lines_build_full_size(ctx, field, lg, logs, cols):
             t = x.clone()
             run(t, inv)
             want[inv] = t
-        ctx.set_plan(fid, lg, logs, elems=[16 | VEC] * 3, cols=[cols] * 3)
+        ctx.set_plan(fid, lg, logs, elems=[16 | VEC] * len(logs), cols=[cols] * len(logs))
         for inv in (False, True):
             t = x.clone()
             run(t, inv)
