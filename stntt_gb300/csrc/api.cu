@@ -414,7 +414,7 @@ void shape_pass(PassDesc &d, int field, uint64_t col_limit, uint32_t want_E, uin
 // 1 within 512 threads; 200 KiB of shared memory at most. want_C picks C (0:
 // the most line groups that fit).
 size_t vec_smem(uint32_t V, uint32_t logG, uint32_t logL, uint32_t w) {
-    const uint32_t pb = logG < 3 ? 3 - logG : 0;  // one 16-byte pad per 2^pb points (tile_v.cuh, vpoint)
+    const uint32_t pb = logG < 2 ? 3 - logG : 0;  // one 16-byte pad per 2^pb points (tile_v.cuh, vpoint)
     return ((size_t)V << logG) * (1u << logL) * w + (pb ? (size_t)((1u << logL) >> pb) * 16 : 0);
 }
 

@@ -16,7 +16,8 @@
 //   - shared memory holds the tile point-major, [point][C lines]: each access
 //     moves one thread's 16 bytes; with 8 line groups the 8 threads of a
 //     quarter-warp phase cover one contiguous 128-byte row, so no padding is
-//     needed for any Stockham stride; with 1, 2 or 4 line groups a 16-byte
+//     needed for any Stockham stride; with 4 line groups some strided writes
+//     meet two-way conflicts, and with 2 (the narrowest wide tiles) a 16-byte
 //     pad after every 128 bytes of points keeps strided writes apart;
 //   - the grid covers the lines exactly (the host only picks shapes where C
 //     divides the lines of a sub-problem), so no access is predicated.
@@ -127,12 +128,17 @@ __device__ __forceinline__ void vstore_last(const TileArgs<F> &a, const F &f, co
 // Element offset of a point's C lines in the shared-memory tile. With 8 line
 // groups (128 bytes per point) points are packed. With fewer, a quarter-warp
 // phase (8 threads x 16 bytes) spans 8 / 2^LOGG points, and Stockham writes
-// of points R apart would land on the same banks; one 16-byte pad after every
-// 8 / 2^LOGG points shifts consecutive rows of 128 bytes by a bank quarter
-// (the scheme of the plain build's padding, at 16-byte granularity).
+// of points R apart land on the same banks. With 4 groups that is a two-way
+// conflict on some writes (about 1% of a Goldilocks pass's instructions); a
+// pad costs more index arithmetic than it saves there (Goldilocks 2^24
+// forward + inverse 0.626 ms unpadded, 0.639 ms padded), so points stay
+// packed. With 1 or 2 groups (the wide tiles of two-pass plans) it would be
+// four- to eight-way: one 16-byte pad after every 8 / 2^LOGG points shifts
+// consecutive 128-byte rows by a bank quarter (the plain build's padding
+// scheme, at 16-byte granularity).
 template <int V, int LOGG>
 __device__ __forceinline__ constexpr uint32_t vpoint(uint32_t point) {
-    constexpr uint32_t C = V << LOGG, PB = LOGG < 3 ? 3 - LOGG : 0;
+    constexpr uint32_t C = V << LOGG, PB = LOGG < 2 ? 3 - LOGG : 0;
     return PB ? point * C + (point >> PB) * V : point * C;
 }
 
