@@ -79,7 +79,14 @@ __device__ __forceinline__ void tw_load_v(typename F::TW (&w)[V], const typename
     }
 }
 
-// Where a thread's lines start in HBM.
+// Where a thread's lines start in HBM. Offsets from these pointers (idx *
+// istride, pos * ostride + col0) stay below the points of one sub-problem or
+// transform (at most 2^32), so 32-bit products are exact. The column loads
+// and the Montgomery-table loads use them: with 64-bit products there, the
+// 32-bit column kernels at 64 registers per thread spilled 60 to 140 bytes per
+// thread (ptxas -v), with 32-bit ones the full-table builds spill nothing.
+// The stores and the 8-byte table keep 64-bit products, which spilled least
+// over all instantiations.
 template <class T, int V>
 struct VGeo {
     const T *src[V];   // COL: src[0] = element 0 of the thread's first column; ROW: row v's element 0
@@ -98,7 +105,7 @@ __device__ __forceinline__ void vstore_last(const TileArgs<F> &a, const F &f, co
     if constexpr (COL) {
         if constexpr (FULL4 == 2) {
             static_assert(V == 4, "Montgomery tables serve the 32-bit field");
-            const uint4 w = __ldg(reinterpret_cast<const uint4 *>(a.tw4_mont + (uint64_t)pos * geo.ostride + geo.col0));
+            const uint4 w = __ldg(reinterpret_cast<const uint4 *>(a.tw4_mont + (pos * geo.ostride + geo.col0)));
             v[0] = f.mul_mont(v[0], w.x, a.pinv);
             v[1] = f.mul_mont(v[1], w.y, a.pinv);
             v[2] = f.mul_mont(v[2], w.z, a.pinv);
@@ -112,9 +119,9 @@ __device__ __forceinline__ void vstore_last(const TileArgs<F> &a, const F &f, co
         } else {
 #pragma unroll
             for (int i = 0; i < V; ++i) {
-                const uint64_t e = (uint64_t)(geo.col0 + i) * pos;
-                const uint32_t lo = (uint32_t)(e & ((1ull << a.h) - 1));
-                const uint32_t hi = (uint32_t)(e >> a.h);
+                const uint32_t e = (geo.col0 + i) * pos;  // col * pos < M <= 2^32
+                const uint32_t lo = e & ((1u << a.h) - 1u);
+                const uint32_t hi = e >> a.h;
                 v[i] = f.mul_tw(f.mul_tw(v[i], __ldg(&a.tw4_lo[lo])), __ldg(&a.tw4_hi[hi]));
             }
         }
@@ -164,7 +171,7 @@ __device__ __forceinline__ void vstep(const TileArgs<F> &a, const F &f, typename
             T t[V];
             if constexpr (first) {
                 if constexpr (COL) {
-                    v16_ldg<T, V>(t, geo.src[0] + (uint64_t)idx * geo.istride);
+                    v16_ldg<T, V>(t, geo.src[0] + idx * geo.istride);
                 } else {
 #pragma unroll
                     for (int i = 0; i < V; ++i)
