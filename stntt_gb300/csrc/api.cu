@@ -95,23 +95,29 @@ uint64_t host_tw_entry(int field, uint64_t w, uint32_t p) {
     return (w & 0xffffffffull) | (wp << 32);
 }
 
-cudaError_t launch_tile_vec_gl64(const PassDesc &, const void *, const void *, void *, uint64_t, cudaStream_t);
+cudaError_t launch_tile_vec_gl64f(const PassDesc &, const void *, const void *, void *, uint64_t, cudaStream_t);
+cudaError_t launch_tile_vec_gl64i(const PassDesc &, const void *, const void *, void *, uint64_t, cudaStream_t);
 cudaError_t launch_tile_vec_u32l(const PassDesc &, uint32_t, const void *, const void *, void *, uint64_t,
                                  cudaStream_t);
-cudaError_t preload_vec_gl64();
+cudaError_t preload_vec_gl64f();
+cudaError_t preload_vec_gl64i();
 cudaError_t preload_vec_u32l();
 
 cudaError_t launch_tile_vec(int field, const PassDesc &d, uint32_t p, const void *tables, const void *in, void *out,
                             uint64_t batch, cudaStream_t s) {
-    if (field == kFieldGL)
-        return launch_tile_vec_gl64(d, tables, in, out, batch, s);
+    if (field == kFieldGL)  // built for the two standard roots only (see PassDesc::pow2)
+        return d.pow2 == 1   ? launch_tile_vec_gl64f(d, tables, in, out, batch, s)
+               : d.pow2 == 2 ? launch_tile_vec_gl64i(d, tables, in, out, batch, s)
+                             : cudaErrorNotSupported;
     if (p < (1u << 30))  // the lazy 32-bit field (every findParams prime up to 2^26)
         return launch_tile_vec_u32l(d, p, tables, in, out, batch, s);
     return cudaErrorNotSupported;
 }
 
 cudaError_t preload_vec() {
-    const cudaError_t e = preload_vec_gl64();
+    cudaError_t e = preload_vec_gl64f();
+    if (e == cudaSuccess)
+        e = preload_vec_gl64i();
     return e == cudaSuccess ? preload_vec_u32l() : e;
 }
 
@@ -450,17 +456,20 @@ uint32_t tma_builtin(int field, const PassDesc &d) {
     return 0;
 }
 
-// Largest column-pass sub-problem (log2 points) of a plain-build pass of a
-// call of 2^22+ elements that reads its four-step twiddle from a full table:
-// kFullTwiddleMaxLog, or STNTT_FULL_TWIDDLE_MAX_LOG from the environment
-// (14..26; read once).
-uint32_t full_twiddle_max_log() {
-    static const uint32_t v = [] {
-        const char *e = getenv("STNTT_FULL_TWIDDLE_MAX_LOG");
-        const long x = e ? strtol(e, nullptr, 10) : -1;
-        return (x >= (long)kFullTwiddleMinLog && x <= 26) ? (uint32_t)x : kFullTwiddleMaxLog;
-    }();
-    return v;
+// Largest column-pass sub-problem (log2 points) of a pass of a call of 2^22+
+// elements that reads its four-step twiddle from a full table, for the plain
+// build (kFullTwiddleMaxLog, or STNTT_FULL_TWIDDLE_MAX_LOG from the
+// environment) and the vector-lines build (kFullTwiddleMaxLogVec, or
+// STNTT_FULL_TWIDDLE_MAX_LOG_VEC); 14..26, read once.
+uint32_t env_log_limit(const char *name, uint32_t dflt) {
+    const char *e = getenv(name);
+    const long x = e ? strtol(e, nullptr, 10) : -1;
+    return (x >= (long)kFullTwiddleMinLog && x <= 26) ? (uint32_t)x : dflt;
+}
+uint32_t full_twiddle_max_log(bool vec) {
+    static const uint32_t plain = env_log_limit("STNTT_FULL_TWIDDLE_MAX_LOG", kFullTwiddleMaxLog);
+    static const uint32_t v = env_log_limit("STNTT_FULL_TWIDDLE_MAX_LOG_VEC", kFullTwiddleMaxLogVec);
+    return vec ? v : plain;
 }
 
 // -p^-1 mod 2^32 for odd p (Newton's iteration doubles the correct low bits).
@@ -538,6 +547,10 @@ int build_plan(stntt_ctx *ctx, Plan &pl, int field, uint32_t log_n, uint32_t p, 
             for (uint32_t j = 0; j < L / 2; ++j)
                 d.wR[j * 16 / L] = host_tw_entry(field, fpow(field, wL, j, p), p);
         }
+        if (field == kFieldGL && log_n >= 4) {
+            const uint64_t w16 = fpow(field, root_dir, n >> 4, p);
+            d.pow2 = w16 == host_gl_pow(2, 156) ? 1 : w16 == host_gl_pow(2, 36) ? 2 : 0;
+        }
         d.scale = host_tw_entry(field, ninv, p);
         uint64_t col_limit;
         if (i + 1 < K) {
@@ -574,10 +587,10 @@ int build_plan(stntt_ctx *ctx, Plan &pl, int field, uint32_t log_n, uint32_t p, 
         // streams from HBM beside the data and still wins (measured on GB300,
         // forward + inverse: Goldilocks 2^24 0.669 -> 0.631 ms, 2^22 0.186 ->
         // 0.176 ms, 32-bit 2^26 1.015 -> 0.994 ms), at n * 8 bytes of table per
-        // plan. STNTT_FULL_TWIDDLE_MAX_LOG (14..26) moves the limit of the
-        // other passes of calls of 2^22+ elements.
+        // plan. STNTT_FULL_TWIDDLE_MAX_LOG and STNTT_FULL_TWIDDLE_MAX_LOG_VEC
+        // (14..26) move the limits of calls of 2^22+ elements.
         if (d.mode == kModeCol && d.logM >= kFullTwiddleMinLog &&
-            d.logM <= (small_call ? kFullTwiddleMaxLogSmall : d.vec ? kFullTwiddleMaxLogVec : full_twiddle_max_log())) {
+            d.logM <= (small_call ? kFullTwiddleMaxLogSmall : full_twiddle_max_log(d.vec != 0))) {
             // Beyond 2^20 points the 32-bit table streams from HBM: there its
             // entries are 4-byte Montgomery values instead of 8-byte Shoup
             // pairs (a 2^26-point table: 256 MiB instead of 512 MiB to read

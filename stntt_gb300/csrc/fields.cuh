@@ -12,6 +12,7 @@
 // All values are kept canonical (< p).
 #pragma once
 #include <cstdint>
+#include <type_traits>
 
 namespace stntt {
 
@@ -161,6 +162,93 @@ struct FieldGL {
     __device__ __forceinline__ static T tw_value(TW w) { return w; }
     __device__ __forceinline__ T sub_lazy(T a, T b) const { return sub(a, b); }
     __device__ __forceinline__ T canon(T a) const { return a; }
+
+    // x * 2^e mod p for 0 < e < 96 (any 64-bit x; canonical result), with e
+    // a constant once the caller's loops are unrolled. The 16th roots of
+    // unity mod p are powers of two (2 has order 192: w_16 = 2^(12 k), k
+    // odd), so the radix-16/8/4 internal twiddles need no product: shift x
+    // into limbs (z2:z1:z0 = x * 2^s, s = e mod 32) and fold the limbs above
+    // 2^64 back with 2^64 = 2^32 - 1 and 2^96 = -1. 10 integer ops for e < 32
+    // or e >= 64, 15 for 32 <= e < 64, against 21 for a product.
+    __device__ __forceinline__ T mul_pow2(T x, int e) const {
+        const uint32_t x0 = (uint32_t)x, x1 = (uint32_t)(x >> 32);
+        const int s = e & 31;
+        const uint32_t z0 = x0 << s;
+        const uint32_t z1 = s ? __funnelshift_l(x0, x1, s) : x1;
+        const uint32_t z2 = s ? x1 >> (32 - s) : 0u;
+        uint32_t r0, r1;
+        if (e < 32) {
+            // (z1:z0) + z2 (2^32 - 1) = (z1:z0) - (p - z2 (2^32 - 1)), and
+            // p - z2 (2^32 - 1) = ~z2 * 2^32 + (z2 + 1) for z2 < 2^31
+            asm("{\n\t"
+                ".reg .u32 m;\n\t"
+                "sub.cc.u32 %0, %2, %4;\n\t"
+                "subc.cc.u32 %1, %3, %5;\n\t"
+                "subc.u32 m, 0, 0;\n\t"
+                "sub.cc.u32 %0, %0, m;\n\t"
+                "subc.u32 %1, %1, 0;\n\t"
+                "}"
+                : "=&r"(r0), "=&r"(r1)
+                : "r"(z0), "r"(z1), "r"(z2 + 1u), "r"(~z2));
+        } else if (e < 64) {
+            // z 2^32 = z0 2^32 + z1 2^64 + z2 2^96 = (z0 + z1) 2^32 - z1 - z2;
+            // with c the carry of z0 + z1 (worth 2^64 = 2^32 - 1):
+            // ((z0 + z1 mod 2^32) + c) 2^32 - (z1 + z2 + c), no limb overflows
+            asm("{\n\t"
+                ".reg .u32 sl, c, a1, b0, b1, m;\n\t"
+                "add.cc.u32 sl, %2, %3;\n\t"
+                "addc.u32 c, 0, 0;\n\t"
+                "add.u32 a1, sl, c;\n\t"
+                "add.cc.u32 b0, %3, %4;\n\t"
+                "addc.u32 b1, 0, 0;\n\t"
+                "add.cc.u32 b0, b0, c;\n\t"
+                "addc.u32 b1, b1, 0;\n\t"
+                "sub.cc.u32 %0, 0, b0;\n\t"
+                "subc.cc.u32 %1, a1, b1;\n\t"
+                "subc.u32 m, 0, 0;\n\t"
+                "sub.cc.u32 %0, %0, m;\n\t"
+                "subc.u32 %1, %1, 0;\n\t"
+                "}"
+                : "=&r"(r0), "=&r"(r1)
+                : "r"(z0), "r"(z1), "r"(z2));
+        } else {
+            // z 2^64 = z0 2^64 + z1 2^96 + z2 2^128 = z0 2^32 - (z2 2^32 + z0 + z1)
+            asm("{\n\t"
+                ".reg .u32 b0, b1, m;\n\t"
+                "add.cc.u32 b0, %2, %3;\n\t"
+                "addc.u32 b1, %4, 0;\n\t"
+                "sub.cc.u32 %0, 0, b0;\n\t"
+                "subc.cc.u32 %1, %2, b1;\n\t"
+                "subc.u32 m, 0, 0;\n\t"
+                "sub.cc.u32 %0, %0, m;\n\t"
+                "subc.u32 %1, %1, 0;\n\t"
+                "}"
+                : "=&r"(r0), "=&r"(r1)
+                : "r"(z0), "r"(z1), "r"(z2));
+        }
+        return ((uint64_t)r1 << 32) | r0;
+    }
 };
+
+// Goldilocks with the transform's radix-16 root fixed at compile time, so
+// that the internal twiddles of the register DFTs are shifts (mul_pow2):
+// DIR = +1 for w_16 = 7^((p-1)/16) = 2^156 (every forward transform: the root
+// of 2^k points is 7^((p-1)/2^k)), -1 for its inverse 2^36. The host picks
+// these types only when a pass's w_16 is that value.
+template <int DIR>
+struct FieldGLPow2 : FieldGL {
+    static constexpr int kDir = DIR;
+    // w_16^q = (-1)^neg 2^e, e < 96, for q = 1..7
+    __device__ __forceinline__ static constexpr int w16_exp(int q) {
+        return ((DIR > 0 ? 156 : 36) * q) % 192;
+    }
+};
+using FieldGLF = FieldGLPow2<1>;
+using FieldGLI = FieldGLPow2<-1>;
+
+template <class F>
+struct IsPow2Field : std::false_type {};
+template <int DIR>
+struct IsPow2Field<FieldGLPow2<DIR>> : std::true_type {};
 
 }  // namespace stntt

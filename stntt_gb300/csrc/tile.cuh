@@ -108,9 +108,16 @@ __device__ __forceinline__ void dft_reg(const F &f, typename F::T *x, const type
 #pragma unroll
             for (int j = 0; j < h; ++j) {
                 const typename F::T a = x[base + j], b = x[base + j + h];
-                const typename F::T d = j == 0 ? f.sub(a, b) : f.sub_lazy(a, b);
-                x[base + j] = f.add(a, b);
-                x[base + j + h] = j == 0 ? d : f.mul_tw(d, w16[j * (16 / (2 * h))]);
+                if constexpr (IsPow2Field<F>::value) {
+                    // w_16^q = +-2^e: the sign by the order of the subtraction
+                    const int q = j * (16 / (2 * h)), e = F::w16_exp(q);
+                    x[base + j] = f.add(a, b);
+                    x[base + j + h] = j == 0 ? f.sub(a, b) : f.mul_pow2(e >= 96 ? f.sub(b, a) : f.sub(a, b), e % 96);
+                } else {
+                    const typename F::T d = j == 0 ? f.sub(a, b) : f.sub_lazy(a, b);
+                    x[base + j] = f.add(a, b);
+                    x[base + j + h] = j == 0 ? d : f.mul_tw(d, w16[j * (16 / (2 * h))]);
+                }
             }
         }
     }
