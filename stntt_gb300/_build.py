@@ -21,8 +21,9 @@ INCLUDE = PKG.parent / "include"
 OUT = PKG / "_lib" / platform.machine()  # x86_64 here, aarch64 on the GPU hosts
 SO = OUT / "libstntt.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["api.cu", "kernels_u32.cu", "kernels_u32l.cu", "kernels_gl64.cu", "kernels_tma_gl64.cu",
-           "kernels_tma_u32l.cu", "kernels_v_gl64.cu", "kernels_v_gl64i.cu", "kernels_v_u32l.cu", "kernels_coop.cu", "noalloc.cu", "serve.cu"]
+SOURCES = ["api.cu", "kernels_u32.cu", "kernels_u32l.cu", "kernels_gl64.cu", "kernels_gl64_f.cu", "kernels_gl64_i.cu",
+           "kernels_tma_gl64.cu", "kernels_tma_u32l.cu", "kernels_v_gl64.cu", "kernels_v_gl64i.cu", "kernels_v_u32l.cu",
+           "kernels_coop.cu", "noalloc.cu", "serve.cu"]
 
 
 def nvcc() -> str:

@@ -547,9 +547,9 @@ int build_plan(stntt_ctx *ctx, Plan &pl, int field, uint32_t log_n, uint32_t p, 
             for (uint32_t j = 0; j < L / 2; ++j)
                 d.wR[j * 16 / L] = host_tw_entry(field, fpow(field, wL, j, p), p);
         }
-        if (field == kFieldGL && log_n >= 4) {
-            const uint64_t w16 = fpow(field, root_dir, n >> 4, p);
-            d.pow2 = w16 == host_gl_pow(2, 156) ? 1 : w16 == host_gl_pow(2, 36) ? 2 : 0;
+        if (field == kFieldGL) {  // the standard roots 7^((p-1)/n) and their inverses: w_16 = 2^156 / 2^36
+            const uint64_t fwd = host_gl_pow(7, (GL_P - 1) >> log_n);
+            d.pow2 = root_dir == fwd ? 1 : root_dir == host_gl_pow(fwd, GL_P - 2) ? 2 : 0;
         }
         d.scale = host_tw_entry(field, ninv, p);
         uint64_t col_limit;
@@ -1912,6 +1912,10 @@ int build_part(stntt_ctx *ctx, stntt_batch *bt, int field, const std::vector<con
         int rc = get_plan(ctx, field, ck.log_n, ck.p, root, (int)ck.dir, &pl, kPlanBatched);
         if (rc)
             return rc;
+        if (field == kFieldGL)  // the batched kernel serves the two standard roots (TileArgs::pow2)
+            for (const PassDesc &d : pl->passes)
+                if (d.pow2 == 0)
+                    return fail(ctx, STNTT_EUNSUPPORTED, "batch: Goldilocks root without a kernel build");
         const size_t J = cj.size();
         const size_t data_off = ptrs.size();
         for (const stntt_job *j : cj)

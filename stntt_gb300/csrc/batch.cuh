@@ -15,6 +15,9 @@
 // (src/cuda/ntt/ntt_kernel.cuh:31-39: one n per launch, transforms laid along
 // blockDim.y) to mixed sizes, fields' parameters and directions.
 #pragma once
+#include <cstring>
+#include <type_traits>
+
 #include "tile.cuh"
 
 namespace stntt {
@@ -49,6 +52,51 @@ __device__ __noinline__ void batch_item_l(const TileArgs<F> &a, uint64_t blk, ty
     tile_run_l<F, LOGL>(a, blk, sm);
 }
 
+// Tiles of other lengths (2^1..2^3 points: single-pass jobs of up to 8 points).
+template <class F>
+__device__ __noinline__ void batch_item_small(const TileArgs<F> &sa, uint64_t blk, typename F::T *sm) {
+    switch (sa.logL & 3) {
+    case 0: tile_run<F, 16, 0>(sa, blk, sm); break;
+    case 1: tile_run<F, 16, 1>(sa, blk, sm); break;
+    case 2: tile_run<F, 16, 2>(sa, blk, sm); break;
+    default: tile_run<F, 16, 3>(sa, blk, sm); break;
+    }
+}
+
+// One item of any tile length (every item: 16 elements per thread).
+template <class F>
+__device__ __forceinline__ void batch_item(const TileArgs<F> &sa, uint64_t blk, typename F::T *sm) {
+    switch (sa.logL) {
+    case 4: batch_item_l<F, 4>(sa, blk, sm); break;
+    case 5: batch_item_l<F, 5>(sa, blk, sm); break;
+    case 6: batch_item_l<F, 6>(sa, blk, sm); break;
+    case 7: batch_item_l<F, 7>(sa, blk, sm); break;
+    case 8: batch_item_l<F, 8>(sa, blk, sm); break;
+    case 9: batch_item_l<F, 9>(sa, blk, sm); break;
+    case 10: batch_item_l<F, 10>(sa, blk, sm); break;
+    case 11: batch_item_l<F, 11>(sa, blk, sm); break;
+    case 12: batch_item_l<F, 12>(sa, blk, sm); break;
+    case 13: batch_item_l<F, 13>(sa, blk, sm); break;
+    default: batch_item_small<F>(sa, blk, sm); break;
+    }
+}
+
+// The current item's descriptor in shared memory. Goldilocks launches mix
+// directions, so their items get the descriptor as the direction-specialised
+// field type (FieldGLF / FieldGLI: shift-only internal twiddles; same
+// layout), chosen per item by TileArgs::pow2 (the host admits only the two
+// standard roots).
+template <class F>
+struct BatchArgsSm {
+    TileArgs<F> a;
+};
+template <>
+struct BatchArgsSm<FieldGL> {
+    TileArgs<FieldGL> a;
+    TileArgs<FieldGLF> f;
+    TileArgs<FieldGLI> i;
+};
+
 template <class F, int MINB = 2>
 __global__ void __launch_bounds__(kBatchThreads, MINB) batch_kernel(const TileArgs<F> *__restrict__ args,
                                                               const BatchItem *__restrict__ items,
@@ -56,7 +104,8 @@ __global__ void __launch_bounds__(kBatchThreads, MINB) batch_kernel(const TileAr
                                                               BatchCtl *ctl, unsigned int spin_limit) {
     using T = typename F::T;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ TileArgs<F> sa;
+    __shared__ BatchArgsSm<F> sargs;
+    TileArgs<F> &sa = sargs.a;
     __shared__ unsigned long long s_item;
     __shared__ int s_ok;
     T *sm = reinterpret_cast<T *>(smem_raw);
@@ -85,27 +134,23 @@ __global__ void __launch_bounds__(kBatchThreads, MINB) batch_kernel(const TileAr
             }
             s_ok = ok;
             sa = args[bi.args];
+            if constexpr (std::is_same_v<F, FieldGL>) {
+                static_assert(sizeof(TileArgs<FieldGLF>) == sizeof(TileArgs<FieldGL>), "same descriptor layout");
+                if (sa.pow2 == 2)
+                    memcpy(&sargs.i, &sa, sizeof(sa));
+                else
+                    memcpy(&sargs.f, &sa, sizeof(sa));
+            }
         }
         __syncthreads();
         if (s_ok) {
-            switch (sa.logL) {  // every item: 16 elements per thread
-            case 4: batch_item_l<F, 4>(sa, bi.blk, sm); break;
-            case 5: batch_item_l<F, 5>(sa, bi.blk, sm); break;
-            case 6: batch_item_l<F, 6>(sa, bi.blk, sm); break;
-            case 7: batch_item_l<F, 7>(sa, bi.blk, sm); break;
-            case 8: batch_item_l<F, 8>(sa, bi.blk, sm); break;
-            case 9: batch_item_l<F, 9>(sa, bi.blk, sm); break;
-            case 10: batch_item_l<F, 10>(sa, bi.blk, sm); break;
-            case 11: batch_item_l<F, 11>(sa, bi.blk, sm); break;
-            case 12: batch_item_l<F, 12>(sa, bi.blk, sm); break;
-            case 13: batch_item_l<F, 13>(sa, bi.blk, sm); break;
-            default:
-                switch (sa.logL & 3) {
-                case 0: tile_run<F, 16, 0>(sa, bi.blk, sm); break;
-                case 1: tile_run<F, 16, 1>(sa, bi.blk, sm); break;
-                case 2: tile_run<F, 16, 2>(sa, bi.blk, sm); break;
-                default: tile_run<F, 16, 3>(sa, bi.blk, sm); break;
-                }
+            if constexpr (std::is_same_v<F, FieldGL>) {
+                if (sa.pow2 == 2)
+                    batch_item<FieldGLI>(sargs.i, bi.blk, sm);
+                else
+                    batch_item<FieldGLF>(sargs.f, bi.blk, sm);
+            } else {
+                batch_item<F>(sa, bi.blk, sm);
             }
         }
         __threadfence();  // this item's stores before the signal below

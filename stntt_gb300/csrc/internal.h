@@ -50,9 +50,10 @@ struct PassDesc {
     // Montgomery entries (w * 2^32 mod p) instead of Shoup pairs; the plain
     // build, which cannot read it, takes the two-level tables instead.
     uint32_t full_mont = 0, pinv = 0;
-    // Goldilocks: 1 when the transform's w_16 is 2^156 (the forward root), 2
-    // when it is 2^36 (the inverse), else 0; kernels built on FieldGLPow2
-    // (shift-only internal twiddles) serve only passes with 1 or 2.
+    // Goldilocks: 1 when the transform's root is the standard forward root
+    // 7^((p-1)/n) (then w_16 = 2^156), 2 when it is its inverse (w_16 =
+    // 2^36), else 0; the kernels built on FieldGLPow2 (shift-only internal
+    // twiddles) serve only passes with 1 or 2.
     uint32_t pow2 = 0;
 };
 

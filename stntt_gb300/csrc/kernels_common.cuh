@@ -207,6 +207,7 @@ void fill_args(TileArgs<F> &a, const PassDesc &d, uint32_t p, const void *tables
     a.tw4_full = (d.full_off == ~0ull || d.full_mont) ? nullptr : tab + d.full_off;
     a.tw4_mont = (d.full_off != ~0ull && d.full_mont) ? reinterpret_cast<const uint32_t *>(tab + d.full_off) : nullptr;
     a.pinv = d.pinv;
+    a.pow2 = d.pow2;
     for (int j = 0; j < 8; ++j)
         std::memcpy(&a.wR[j], &d.wR[j], sizeof(TW));
     std::memcpy(&a.scale, &d.scale, sizeof(TW));
@@ -239,9 +240,15 @@ cudaError_t launch_tma_u32l(const PassDesc &d, const TileArgs<FieldU32L> &a, uin
 template <class F>
 cudaError_t launch_tma(const PassDesc &d, const TileArgs<F> &a, uint64_t batch, uint64_t tiles, int *err,
                        cudaStream_t s) {
-    if constexpr (std::is_same_v<F, FieldGL>)
+    if constexpr (std::is_same_v<F, FieldGL>) {
         return launch_tma_gl64(d, a, batch, tiles, err, s);
-    else if constexpr (std::is_same_v<F, FieldU32L>)
+    } else if constexpr (IsPow2Field<F>::value) {
+        // the staged kernel keeps product internal twiddles (same descriptor)
+        static_assert(sizeof(TileArgs<F>) == sizeof(TileArgs<FieldGL>), "same descriptor layout");
+        TileArgs<FieldGL> g;
+        std::memcpy(&g, &a, sizeof(g));
+        return launch_tma_gl64(d, g, batch, tiles, err, s);
+    } else if constexpr (std::is_same_v<F, FieldU32L>)
         return launch_tma_u32l(d, a, batch, tiles, err, s);
     else
         return cudaErrorNotSupported;
@@ -487,8 +494,12 @@ cudaError_t preload_tiles_t() {
     for (cudaError_t e : list)
         if (e != cudaSuccess)
             return e;
-    int blocks = 0;
-    return batch_prepare_t<F>(0, &blocks);
+    if constexpr (IsPow2Field<F>::value) {
+        return cudaSuccess;  // the batched kernel runs FieldGL (its launches mix directions)
+    } else {
+        int blocks = 0;
+        return batch_prepare_t<F>(0, &blocks);
+    }
 }
 
 // Twiddle entry from a residue (u32: Shoup pair {w, floor(w 2^32 / p)}).

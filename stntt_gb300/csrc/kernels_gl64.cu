@@ -32,9 +32,29 @@ __global__ void fill_uniform_gl64_kernel(uint64_t *out, size_t count, uint64_t s
     }
 }
 
+// The single-transform tile and cluster kernels are built per direction
+// (FieldGLF / FieldGLI: shift-only internal twiddles) in kernels_gl64_f.cu and
+// kernels_gl64_i.cu; every Goldilocks plan has one of the two roots
+// (PassDesc::pow2). The batched kernel, whose launches mix directions, keeps
+// FieldGL.
+cudaError_t launch_tile_gl64f(const PassDesc &, uint32_t, const void *, const void *, void *, uint64_t, cudaStream_t,
+                              const void *, int *);
+cudaError_t launch_tile_gl64i(const PassDesc &, uint32_t, const void *, const void *, void *, uint64_t, cudaStream_t,
+                              const void *, int *);
+cudaError_t launch_cluster_gl64f(const PassDesc &, const PassDesc &, uint32_t, const void *, const void *, void *,
+                                 uint64_t, uint32_t, uint32_t, size_t, uint32_t, cudaStream_t);
+cudaError_t launch_cluster_gl64i(const PassDesc &, const PassDesc &, uint32_t, const void *, const void *, void *,
+                                 uint64_t, uint32_t, uint32_t, size_t, uint32_t, cudaStream_t);
+cudaError_t preload_gl64f();
+cudaError_t preload_gl64i();
+
 cudaError_t launch_tile_gl64(const PassDesc &d, uint32_t p, const void *tables, const void *in, void *out,
                     uint64_t batch, cudaStream_t s, const void *in2, int *err) {
-    return launch_tile_t<FieldGL>(d, p, tables, in, out, batch, s, in2, err);
+    if (d.pow2 == 1)
+        return launch_tile_gl64f(d, p, tables, in, out, batch, s, in2, err);
+    if (d.pow2 == 2)
+        return launch_tile_gl64i(d, p, tables, in, out, batch, s, in2, err);
+    return cudaErrorNotSupported;
 }
 
 cudaError_t gen_powers_gl64(void *out, uint64_t count, uint64_t base, uint64_t scale, cudaStream_t s) {
@@ -79,15 +99,16 @@ cudaError_t batch_launch_gl64(const void *args, const void *items, unsigned long
 
 // ---- integer throughput probe ------------------------------------------------
 // The tile kernel's arithmetic without its memory traffic: every thread runs
-// the radix-16 step (15 twiddle products, then the 16-point DIF network with
-// 17 products) on 16 register values, `reps` times, and writes one checksum.
+// the radix-16 step (15 twiddle products, then the 16-point DIF network whose
+// 17 internal twiddles are shifts, as in the tile kernels: dft_reg over
+// FieldGLF) on 16 register values, `reps` times, and writes one checksum.
 // Measures the Goldilocks butterfly rate this GPU sustains: the integer
 // roofline the NTT kernels are compared with.
 namespace stntt {
 
 __global__ void __launch_bounds__(256) gl_butterfly_probe(uint64_t *out, int reps, uint64_t w1, uint64_t w2,
                                                           uint64_t w3) {
-    FieldGL f;
+    FieldGLF f;
     uint64_t x[16];
     uint64_t seed = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * 0x9E3779B97F4A7C15ull + 1;
 #pragma unroll
@@ -100,17 +121,7 @@ __global__ void __launch_bounds__(256) gl_butterfly_probe(uint64_t *out, int rep
 #pragma unroll
         for (int i = 1; i < 16; ++i)
             x[i] = f.mul(x[i], w[i & 7]);
-#pragma unroll
-        for (int h = 8; h >= 1; h >>= 1)
-#pragma unroll
-            for (int base = 0; base < 16; base += 2 * h)
-#pragma unroll
-                for (int j = 0; j < h; ++j) {
-                    const uint64_t a = x[base + j], b = x[base + j + h];
-                    x[base + j] = f.add(a, b);
-                    const uint64_t d = f.sub(a, b);
-                    x[base + j + h] = j == 0 ? d : f.mul(d, w[j * (16 / (2 * h))]);
-                }
+        dft_reg<FieldGLF, 16>(f, x, w);
     }
     uint64_t acc = 0;
 #pragma unroll
@@ -127,9 +138,12 @@ cudaError_t launch_gl_probe(uint64_t *out, unsigned blocks, int reps, cudaStream
 
 cudaError_t preload_gl64() {
     cudaFuncAttributes at;
-    cudaError_t e = preload_tiles_t<FieldGL>();
+    cudaError_t e = preload_gl64f();
     if (e == cudaSuccess)
-        e = preload_clusters_t<FieldGL>();
+        e = preload_gl64i();
+    int blocks = 0;
+    if (e == cudaSuccess)
+        e = batch_prepare_t<FieldGL>(0, &blocks);
     if (e == cudaSuccess)
         e = cudaFuncGetAttributes(&at, gen_powers_kernel<FieldGL>);
     if (e == cudaSuccess)
@@ -151,9 +165,11 @@ cudaError_t gen_four_step_gl64(void *out, const void *lo, const void *hi, uint32
 cudaError_t launch_cluster_gl64(const PassDesc &d1, const PassDesc &d2, uint32_t p, const void *tables,
                                 const void *in, void *out, uint64_t batch, uint32_t xoff, uint32_t xs, size_t smem,
                                 uint32_t log_k, cudaStream_t s) {
-    return launch_cluster_t<FieldGL>(d1, d2, p, tables, in, out, batch, xoff, xs, smem, log_k, s);
+    if (d1.pow2 == 1 && d2.pow2 == 1)
+        return launch_cluster_gl64f(d1, d2, p, tables, in, out, batch, xoff, xs, smem, log_k, s);
+    if (d1.pow2 == 2 && d2.pow2 == 2)
+        return launch_cluster_gl64i(d1, d2, p, tables, in, out, batch, xoff, xs, smem, log_k, s);
+    return cudaErrorNotSupported;
 }
-
-int cluster_max_size() { return cluster_max_size_t<FieldGL>(); }
 
 }  // namespace stntt

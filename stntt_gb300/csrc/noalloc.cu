@@ -151,6 +151,7 @@ extern "C" int stntt_ntt_gl64_noalloc(const uint64_t *d_in, uint64_t *d_out, uin
                 d.wR[j * 16 / L] = host_gl_pow(wL, j);
         }
         d.scale = ninv;
+        d.pow2 = dir == STNTT_INVERSE ? 2 : 1;  // the standard roots (see PassDesc::pow2)
         uint64_t col_limit;
         if (i + 1 < K) {
             d.mode = kModeCol;

@@ -69,6 +69,9 @@ struct TileArgs {
     // and pinv = -p^-1 mod 2^32.
     const uint32_t *tw4_mont;
     uint32_t pinv;
+    // Goldilocks: PassDesc::pow2 (1 forward root, 2 inverse root, 0 other);
+    // the batched kernel picks the direction-specialised field type by it.
+    uint32_t pow2;
 };
 
 template <class F>
@@ -88,6 +91,8 @@ struct Pad<FieldGL> {
     static constexpr uint32_t PS = 4;
     static __device__ __forceinline__ uint32_t at(uint32_t i) { return i + (i >> 4); }
 };
+template <int DIR>
+struct Pad<FieldGLPow2<DIR>> : Pad<FieldGL> {};
 
 template <int LOGR>
 __host__ __device__ constexpr int bit_reverse(int r) {

@@ -815,3 +815,34 @@ def test_cooperative_two_pass_launch(ctx, field, lg):
         ctx.clear_plans()
         from stntt_gb300 import tune
         tune.apply_cache(ctx)
+
+
+GL_P = (1 << 64) - (1 << 32) + 1
+GL_EDGE = np.array([0, 1, 2, GL_P - 1, GL_P - 2, (1 << 32) - 1, 1 << 32, (1 << 32) + 1, 1 << 63, (1 << 63) - 1,
+                    GL_P - (1 << 32), (GL_P - 1) // 2, 0xFFFFFFFF00000000, 0x00000000FFFFFFFF, 0x8000000080000000,
+                    0x7FFFFFFF7FFFFFFF], dtype=np.uint64)
+
+
+@pytest.mark.parametrize("lg,logs,elems,cols", [(16, [8, 8], 8, 8), (16, [8, 8], 16, 16), (22, [7, 8, 7], 8, 8),
+                                                (20, [10, 10], 16, 4)])
+def test_gl64_edge_values(ctx, lg, logs, elems, cols):
+    """Goldilocks passes with shift-only internal twiddles (radix-4/8 with 8
+    points per line, radix-16 with 16: every w_16^q = +-2^e) on inputs built
+    from limb-boundary residues (0, 1, p - 1, 2^32 - 1, 2^32, 2^63, ...):
+    both directions against the oracle, and the tuned plan as well."""
+    n = 1 << lg
+    rng = np.random.default_rng(lg)
+    x = GL_EDGE[rng.integers(0, len(GL_EDGE), n)]
+    x[: len(GL_EDGE)] = GL_EDGE
+    try:
+        for plan in ("tuned", "vec"):
+            if plan == "vec":
+                ctx.set_plan(st.FIELD_GL64, lg, logs, elems=[elems | VEC] * len(logs), cols=[cols] * len(logs))
+            for inv in (False, True):
+                d = dev64(x)
+                ctx.ntt_gl64(d, lg, 1, inverse=inv)
+                assert np.array_equal(host64(d), O.ntt_gl64(x, inverse=inv, threads=8)), (plan, inv)
+    finally:
+        ctx.clear_plans()
+        from stntt_gb300 import tune
+        tune.apply_cache(ctx)
