@@ -114,6 +114,12 @@ int stntt_call_info(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t batch, u
  * cols then gives the lines per CTA (4 or 8 times V, V = 4 for the 32-bit
  * field and 2 for Goldilocks). */
 #define STNTT_PASS_VEC 0x100u
+/* elems flag, with STNTT_PASS_VEC and 8 points per line: the vector-lines
+ * cluster build for passes of 2^11..2^13 points (each line's DFT spread over
+ * the 8 CTAs of a thread-block cluster through distributed shared memory),
+ * which makes two-pass plans of 2^22..2^26 points possible; cols gives the
+ * lines per cluster (4 or 8 times V). */
+#define STNTT_PASS_CLUSTER 0x200u
 
 /* Override the plan for one (field, log_n): npasses HBM passes (1..4) with
  * tile lengths 2^pass_logs[i] (summing to log_n, each <= 13; npasses <= 3), elements per

@@ -39,6 +39,7 @@ FORWARD, INVERSE = 0, 1
 FIELD_U32, FIELD_GL64 = 0, 1
 FLAG_REF_WRAP = 0x1
 PASS_VEC = 0x100  # STNTT_PASS_VEC: elems flag for the vector-lines build of a pass
+PASS_CLUSTER = 0x200  # STNTT_PASS_CLUSTER: with PASS_VEC | 8, the vector-lines cluster build (2^11..2^13 points)
 STATUS = {0: "OK", 1: "EINVAL", 2: "ENOMEM", 3: "ECUDA", 4: "ETIMEOUT", 5: "EUNSUPPORTED"}
 
 

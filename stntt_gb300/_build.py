@@ -23,6 +23,7 @@ SO = OUT / "libstntt.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["api.cu", "kernels_u32.cu", "kernels_u32l.cu", "kernels_gl64.cu", "kernels_gl64_f.cu", "kernels_gl64_i.cu",
            "kernels_tma_gl64.cu", "kernels_tma_u32l.cu", "kernels_v_gl64.cu", "kernels_v_gl64i.cu", "kernels_v_u32l.cu",
+           "kernels_vc_gl64.cu", "kernels_vc_u32l.cu",
            "kernels_coop.cu", "noalloc.cu", "serve.cu"]
 
 

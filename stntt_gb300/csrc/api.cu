@@ -103,8 +103,30 @@ cudaError_t preload_vec_gl64f();
 cudaError_t preload_vec_gl64i();
 cudaError_t preload_vec_u32l();
 
+cudaError_t launch_tile_vc_gl64(const PassDesc &, const void *, const void *, void *, uint64_t, cudaStream_t);
+cudaError_t launch_tile_vc_u32l(const PassDesc &, uint32_t, const void *, const void *, void *, uint64_t,
+                                cudaStream_t);
+cudaError_t preload_vc_gl64();
+cudaError_t preload_vc_u32l();
+
+cudaError_t launch_tile_vc(int field, const PassDesc &d, uint32_t p, const void *tables, const void *in, void *out,
+                           uint64_t batch, cudaStream_t s) {
+    if (field == kFieldGL)
+        return launch_tile_vc_gl64(d, tables, in, out, batch, s);
+    if (p < (1u << 30))
+        return launch_tile_vc_u32l(d, p, tables, in, out, batch, s);
+    return cudaErrorNotSupported;
+}
+
+cudaError_t preload_vc() {
+    const cudaError_t e = preload_vc_gl64();
+    return e == cudaSuccess ? preload_vc_u32l() : e;
+}
+
 cudaError_t launch_tile_vec(int field, const PassDesc &d, uint32_t p, const void *tables, const void *in, void *out,
                             uint64_t batch, cudaStream_t s) {
+    if (d.vcl)
+        return launch_tile_vc(field, d, p, tables, in, out, batch, s);
     if (field == kFieldGL)  // built for the two standard roots only (see PassDesc::pow2)
         return d.pow2 == 1   ? launch_tile_vec_gl64f(d, tables, in, out, batch, s)
                : d.pow2 == 2 ? launch_tile_vec_gl64i(d, tables, in, out, batch, s)
@@ -118,6 +140,8 @@ cudaError_t preload_vec() {
     cudaError_t e = preload_vec_gl64f();
     if (e == cudaSuccess)
         e = preload_vec_gl64i();
+    if (e == cudaSuccess)
+        e = preload_vc();
     return e == cudaSuccess ? preload_vec_u32l() : e;
 }
 
@@ -448,6 +472,35 @@ void shape_pass_vec(PassDesc &d, int field, uint64_t col_limit, uint32_t want_E,
     d.vsmem = vec_smem(V, logG, d.logL, w);
 }
 
+// The vector-lines cluster build of a pass (tile_vc.cuh), when asked for
+// (STNTT_PASS_CLUSTER with STNTT_PASS_VEC): passes of 2^11..2^13 points, 8
+// points per line, clusters of 8 CTAs, the first phase over 2^ceil(logL/2)
+// points; C = V * 4 or V * 8 lines per cluster, one CTA's threads within 1024
+// and its registers (64 or 80 per thread) within the SM's 65536.
+void shape_pass_vc(PassDesc &d, int field, uint64_t col_limit, uint32_t want_C) {
+    d.vcl = 0;
+    if (d.logL < 11 || d.logL > 13 || d.do_scale || d.logL >= d.logN)
+        return;
+    const uint32_t V = field == kFieldGL ? 2 : 4, w = field == kFieldGL ? 8 : 4, regs = field == kFieldGL ? 80 : 64;
+    const uint32_t logK = 3, log1 = (d.logL + 1) / 2;
+    uint32_t logG = want_C == (V << 2) ? 2 : 3;
+    const auto threads = [&](uint32_t g) { return (1u << (d.logL - log1 - logK + g)) * ((1u << log1) / 8); };
+    const auto smem = [&](uint32_t g) { return ((size_t)V << g) * (1u << d.logL) * w >> logK; };
+    while (logG > 2 && (((uint64_t)V << logG) > col_limit || threads(logG) > 1024 || threads(logG) * regs > 65536 ||
+                        smem(logG) > 200 * 1024))
+        --logG;
+    if (((uint64_t)V << logG) > col_limit || threads(logG) > 1024 || threads(logG) * regs > 65536 ||
+        smem(logG) > 200 * 1024)
+        return;
+    d.vec = V;
+    d.vE = 8;
+    d.vlogG = logG;
+    d.vcl = logK;
+    d.vlog1 = log1;
+    d.vthreads = threads(logG);
+    d.vsmem = smem(logG);
+}
+
 // Whether a pass runs TMA-staged (tma.cuh) by default; the kernel still
 // falls back to the plain one where the pass does not allow it.
 uint32_t tma_builtin(int field, const PassDesc &d) {
@@ -577,6 +630,8 @@ int build_plan(stntt_ctx *ctx, Plan &pl, int field, uint32_t log_n, uint32_t p, 
             if (d.mode == kModeRow)
                 col_limit = std::min<uint64_t>(col_limit, 1ull << (log_n - d.logL));
             shape_pass_vec(d, field, col_limit, want_e & 0xffu, spec ? spec->cols[i] : 0);
+            if (want_e & STNTT_PASS_CLUSTER)
+                shape_pass_vc(d, field, col_limit, spec ? spec->cols[i] : 0);
         }
         // Column passes over 2^14..2^20-point sub-problems read the twiddle
         // w_M^(col*pos) from a table laid out like the data: one load and one
@@ -1307,9 +1362,11 @@ int set_plan_for(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t npasses, co
         const uint32_t lg = pass_logs[i], e = elems ? elems[i] : 0, c = cols ? cols[i] : 0;
         if (lg == 0 || lg > 13)
             return fail(ctx, STNTT_EINVAL, "set_plan: each pass length must be 2^1..2^13");
-        const uint32_t eb = e & ~STNTT_PASS_VEC;
+        const uint32_t eb = e & ~(STNTT_PASS_VEC | STNTT_PASS_CLUSTER);
         if ((eb != 0 && eb != 8 && eb != 16 && eb != 32) || ((e & STNTT_PASS_VEC) && eb == 32))
             return fail(ctx, STNTT_EINVAL, "set_plan: elems must be 0, 8, 16 or 32 (STNTT_PASS_VEC with 0, 8 or 16)");
+        if ((e & STNTT_PASS_CLUSTER) && (!(e & STNTT_PASS_VEC) || (eb != 0 && eb != 8)))
+            return fail(ctx, STNTT_EINVAL, "set_plan: STNTT_PASS_CLUSTER goes with STNTT_PASS_VEC and 8 points per line");
         if (c & (c - 1))
             return fail(ctx, STNTT_EINVAL, "set_plan: cols must be 0 or a power of two");
         s.logs.push_back(lg);

@@ -55,6 +55,10 @@ struct PassDesc {
     // 2^36), else 0; the kernels built on FieldGLPow2 (shift-only internal
     // twiddles) serve only passes with 1 or 2.
     uint32_t pow2 = 0;
+    // Vector-lines cluster build (tile_vc.cuh), when vcl != 0: each line's
+    // DFT over the 2^vcl CTAs of a thread-block cluster, first phase of
+    // 2^vlog1 points; vlogG, vthreads and vsmem then describe one CTA.
+    uint32_t vcl = 0, vlog1 = 0;
 };
 
 // ---- launchers (return the CUDA error of the launch) ----------------------
@@ -82,6 +86,10 @@ int cluster_max_size();
 cudaError_t launch_tile_vec(int field, const PassDesc &d, uint32_t p, const void *tables, const void *in, void *out,
                             uint64_t batch, cudaStream_t s);
 cudaError_t preload_vec();
+// The vector-lines cluster build of a pass (tile_vc.cuh, d.vcl != 0).
+cudaError_t launch_tile_vc(int field, const PassDesc &d, uint32_t p, const void *tables, const void *in, void *out,
+                           uint64_t batch, cudaStream_t s);
+cudaError_t preload_vc();
 // Both passes of a two-pass plan in one cooperative launch (coop.cuh): d1 the
 // column pass into ws, d2 the row pass into out, with equal block sizes; bar:
 // the stream's zero-initialised barrier words; err: the device error word.

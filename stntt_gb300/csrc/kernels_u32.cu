@@ -230,7 +230,7 @@ cudaError_t launch_find_params(uint64_t size, uint64_t min_mod, uint64_t *out, c
 }
 
 __global__ void gen_four_step_mont_kernel(uint32_t *out, const uint2 *lo, const uint2 *hi, uint32_t h, uint32_t logS,
-                                          uint64_t count, uint32_t p);
+                                          uint64_t count, uint32_t p, uint2 r32);
 
 cudaError_t preload_u32() {
     cudaFuncAttributes at;
@@ -252,15 +252,19 @@ cudaError_t preload_u32() {
     return e;
 }
 
-// out[pos * S + col] = w_M^(col * pos) * 2^32 mod p (Montgomery form), e = col * pos < M
+// out[pos * S + col] = w_M^(col * pos) * 2^32 mod p (Montgomery form), e = col * pos < M:
+// two Shoup products (lo * hi, then by r32 = the Shoup pair of 2^32 mod p)
+// instead of two 64-bit remainders (2^26 entries: 481 us per table before).
 __global__ void gen_four_step_mont_kernel(uint32_t *out, const uint2 *lo, const uint2 *hi, uint32_t h, uint32_t logS,
-                                          uint64_t count, uint32_t p) {
+                                          uint64_t count, uint32_t p, uint2 r32) {
     const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= count)
         return;
+    FieldU32 f;
+    f.p = p;
     const uint64_t e = (i >> logS) * (i & ((1ull << logS) - 1));
-    const uint64_t w = (uint64_t)lo[e & ((1ull << h) - 1)].x * hi[e >> h].x % p;
-    out[i] = (uint32_t)((w << 32) % p);
+    const uint32_t w = f.mul_tw(lo[e & ((1ull << h) - 1)].x, hi[e >> h]);
+    out[i] = f.mul_tw(w, r32);
 }
 
 cudaError_t gen_four_step_mont_u32(void *out, const void *lo, const void *hi, uint32_t h, uint32_t logS, uint64_t count,
@@ -268,9 +272,12 @@ cudaError_t gen_four_step_mont_u32(void *out, const void *lo, const void *hi, ui
     const uint64_t blocks = (count + 255) / 256;
     if (!blocks)
         return cudaSuccess;
+    const uint32_t r = (uint32_t)((1ull << 32) % p);
+    const uint2 r32 = make_uint2(r, (uint32_t)(((uint64_t)r << 32) / p));
     gen_four_step_mont_kernel<<<(unsigned)blocks, 256, 0, s>>>(static_cast<uint32_t *>(out),
                                                                static_cast<const uint2 *>(lo),
-                                                               static_cast<const uint2 *>(hi), h, logS, count, p);
+                                                               static_cast<const uint2 *>(hi), h, logS, count, p,
+                                                               r32);
     return cudaGetLastError();
 }
 

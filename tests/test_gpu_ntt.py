@@ -846,3 +846,75 @@ def test_gl64_edge_values(ctx, lg, logs, elems, cols):
         ctx.clear_plans()
         from stntt_gb300 import tune
         tune.apply_cache(ctx)
+
+
+CL = st.PASS_CLUSTER
+
+
+@pytest.mark.parametrize("field,lg,logs,cols,batch", [
+    ("gl64", 22, [11, 11], 8, 1),    # every pass in the cluster build, against the oracle
+    ("u32", 22, [11, 11], 16, 1),
+    ("gl64", 20, [11, 9], 16, 2),    # cluster column pass, then a vector-lines row pass
+    ("u32", 21, [9, 12], 32, 1),     # vector-lines column pass, then a cluster row pass
+])
+def test_vector_lines_cluster_pass(ctx, field, lg, logs, cols, batch):
+    """STNTT_PASS_CLUSTER: passes whose line DFTs are spread over the 8 CTAs
+    of a thread-block cluster (distributed shared memory), forward and
+    inverse, against the oracle."""
+    fid = st.FIELD_GL64 if field == "gl64" else st.FIELD_U32
+    elems = [(8 | VEC | CL) if lg_ >= 11 else (8 | VEC) for lg_ in logs]
+    try:
+        ctx.set_plan(fid, lg, logs, elems=elems, cols=[cols] * len(logs))
+        n = 1 << lg
+        for inv in (False, True):
+            if field == "gl64":
+                x = O.uniform_u64(700 + lg, batch * n)
+                d = dev64(x)
+                ctx.ntt_gl64(d, lg, batch, inverse=inv)
+                assert np.array_equal(host64(d), O.ntt_gl64(x, inverse=inv, batch=batch, threads=8)), inv
+            else:
+                p, root = st.params_u32(lg)
+                x = O.uniform_u32(700 + lg, p, batch * n)
+                d = dev32(x)
+                ctx.ntt_u32(d, lg, batch, p, root, inverse=inv)
+                assert np.array_equal(host32(d), O.ntt_u32(x, root, p, inverse=inv, batch=batch, threads=8)), inv
+    finally:
+        ctx.clear_plans()
+        from stntt_gb300 import tune
+        tune.apply_cache(ctx)
+
+
+@pytest.mark.parametrize("field,lg,logs,cols", [("gl64", 24, [12, 12], 8), ("gl64", 24, [12, 12], 16),
+                                                ("u32", 26, [13, 13], 16), ("u32", 26, [13, 13], 32),
+                                                ("u32", 24, [12, 12], 16), ("gl64", 25, [12, 13], 8)])
+def test_vector_lines_cluster_pass_full_size(ctx, field, lg, logs, cols):
+    """Two-pass plans with cluster passes at 2^24..2^26 equal the tuned
+    plan (pinned against the oracle at these sizes) bit for bit, both
+    directions."""
+    fid = st.FIELD_GL64 if field == "gl64" else st.FIELD_U32
+    n = 1 << lg
+    p, root = (0, 0) if field == "gl64" else st.params_u32(lg)
+    if field == "gl64":
+        x = torch.empty(n, dtype=torch.int64, device="cuda")
+        st.fill_uniform_gl64(x, 6)
+        run = lambda t, inv: ctx.ntt_gl64(t, lg, 1, inverse=inv)  # noqa: E731
+    else:
+        x = torch.empty(n, dtype=torch.int32, device="cuda")
+        st.fill_uniform_u32(x, 6, p)
+        run = lambda t, inv: ctx.ntt_u32(t, lg, 1, p, root, inverse=inv)  # noqa: E731
+    try:
+        want = {}
+        for inv in (False, True):
+            t = x.clone()
+            run(t, inv)
+            want[inv] = t
+        ctx.set_plan(fid, lg, logs, elems=[8 | VEC | CL] * len(logs), cols=[cols] * len(logs))
+        for inv in (False, True):
+            t = x.clone()
+            run(t, inv)
+            torch.cuda.synchronize()
+            assert torch.equal(t, want[inv]), inv
+    finally:
+        ctx.clear_plans()
+        from stntt_gb300 import tune
+        tune.apply_cache(ctx)
