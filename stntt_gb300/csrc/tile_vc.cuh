@@ -10,12 +10,14 @@
 //     over j1 of its Q * C sub-lines, loaded from HBM (16 bytes = V lines per
 //     access, as in tile_v.cuh), each output k1 multiplied by w_L^(j2 k1) and
 //     left in its own shared memory, point-major [k1][q][C];
-//   cluster barrier (every CTA's phase-1 results complete and visible);
+//   cluster barrier (every CTA's phase-1 results complete and visible;
+//     arrive and wait split around the phase-2 set-up);
 //   phase 2: CTA r takes k1 in [r P, (r+1) P), P = L1 / K: the L2-point DFTs
 //     over j2, whose inputs (k1, j2) sit in CTA j2 / Q's shared memory and are
 //     read through distributed shared memory, 16 bytes per access; after
-//     those reads a second cluster barrier lets every CTA reuse its buffer
-//     for the rest of phase 2; outputs k = k1 + L1 k2 go to HBM as the
+//     those reads a second cluster barrier (arrive after the reads, wait
+//     after the first DFTs) lets every CTA reuse its buffer for the rest of
+//     phase 2; outputs k = k1 + L1 k2 go to HBM as the
 //     vector-lines pass writes them (four-step twiddle of a column pass,
 //     digit-reversed positions of a row pass).
 // Shared memory per CTA: L * C * w / K bytes; both phases' tiles share it.
@@ -35,10 +37,15 @@ __device__ __forceinline__ uint32_t vc_rank() {
 }
 
 // Every thread of every CTA of the cluster; orders shared-memory accesses
-// across the cluster (release / acquire).
+// across the cluster (release / acquire). The arrive and the wait may be
+// apart: work between them overlaps the other CTAs' arrival.
+__device__ __forceinline__ void vc_cluster_arrive() {
+    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void vc_cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
 __device__ __forceinline__ void vc_cluster_sync() {
-    asm volatile("barrier.cluster.arrive.release.aligned;\n\t"
-                 "barrier.cluster.wait.acquire.aligned;" ::: "memory");
+    vc_cluster_arrive();
+    vc_cluster_wait();
 }
 
 // 16 bytes (V elements) from CTA `rank`'s shared memory at the offset of the
@@ -91,6 +98,8 @@ __device__ __forceinline__ void vcstep(const TileArgs<F> &a, const F &f, typenam
                 x[i][m * R + r] = t[i];
         }
     }
+    if constexpr (SYNC == 2)
+        vc_cluster_arrive();  // this thread's reads are done (release); the DFTs below overlap the others
 #pragma unroll
     for (int m = 0; m < ITEMS; ++m) {
         if constexpr (!FIRST) {
@@ -110,7 +119,7 @@ __device__ __forceinline__ void vcstep(const TileArgs<F> &a, const F &f, typenam
     if constexpr (SYNC == 1)
         __syncthreads();
     else if constexpr (SYNC == 2)
-        vc_cluster_sync();
+        vc_cluster_wait();
 #pragma unroll
     for (int m = 0; m < ITEMS; ++m) {
         const uint32_t t = u + m * U;
@@ -226,7 +235,7 @@ __global__ void __launch_bounds__(vc_threads<LOGL, LOG1, LOGG, LOGK, V>(),
     pdl_enter();
     T x[V][E];
     vcsteps<F, V, E, LOG1, LOGG1, LOG2, 0, 1, false, 0>(a, f, x, sm_g1, u1, load1, store1);
-    vc_cluster_sync();
+    vc_cluster_arrive();  // this CTA's phase-1 results are written (release)
 
     // ---- phase 2: thread = (u2, p, g); line (k1 = rank P + p, lines g V ..)
     const uint32_t g2 = threadIdx.x & ((1u << LOGG2) - 1), u2 = threadIdx.x >> LOGG2;
@@ -248,6 +257,7 @@ __global__ void __launch_bounds__(vc_threads<LOGL, LOG1, LOGG, LOGK, V>(),
         geo.ostride = 1u << logPer;
     }
     const auto store2 = [&](uint32_t k2, T(&v)[V]) { vstore_last<F, V, COL, FULL4>(a, f, geo, k1 + (k2 << LOG1), v); };
+    vc_cluster_wait();  // every CTA's phase-1 results are visible (acquire)
     vcsteps<F, V, E, LOG2, LOGG2, LOG1, 2, 0, true, 0>(a, f, x, sm + g2 * V, u2, load2, store2);
 }
 

@@ -71,18 +71,45 @@ def vec_candidates(field: int, logs: list[int]) -> Iterable[tuple[list[int], lis
                 yield list(logs), list(es), [g * v] * len(logs)
 
 
+def cluster_candidates(field: int, logs: list[int]) -> Iterable[tuple[list[int], list[int], list[int]]]:
+    """The vector-lines cluster build (STNTT_PASS_CLUSTER, 8 points per line)
+    for the 2^11..2^13-point passes of a two-pass split, the other pass in the
+    vector-lines build: 4 or 8 line groups per cluster or CTA, within 1024
+    threads, the SM's 65536 registers (64 or 80 per thread) and 200 KiB of
+    shared memory per CTA."""
+    if len(logs) != 2 or not all(7 <= lg <= 13 for lg in logs) or max(logs) < 11:
+        return
+    v = 2 if field == st.FIELD_GL64 else 4
+    w = 8 if field == st.FIELD_GL64 else 4
+    regs = 80 if field == st.FIELD_GL64 else 64
+    for g in (4, 8):
+        es, ok = [], True
+        for lg in logs:
+            if lg >= 11:
+                log1 = (lg + 1) // 2
+                threads = (g << (lg - log1 - 3)) * ((1 << log1) // 8)
+                ok &= threads <= 1024 and threads * regs <= 65536 and g * v * (1 << lg) * w // 8 <= 200 * 1024
+                es.append(8 | st.PASS_VEC | st.PASS_CLUSTER)
+            else:
+                ok &= lg <= 10
+                es.append(8 | st.PASS_VEC)
+        if ok:
+            yield list(logs), es, [g * v] * 2
+
+
 def candidates(field: int, log_n: int, full: bool = False,
                vec: bool = False) -> Iterable[tuple[list[int], list[int], list[int]]]:
     """Plan shapes to try: every columns-per-CTA choice, 16 or 32 elements per
     thread (and 8 where every pass is 2^7..2^11 points); without `full`, only
     the three most even two-pass splits and the most even three-pass split;
     with `vec`, also the vector-lines build of every two- or three-pass split
-    of 2^7..2^10-point passes."""
+    of 2^7..2^10-point passes, and two-pass splits with cluster passes."""
     sp = splits(log_n)
     if vec:
         for logs in sp:
             if len(logs) >= 2:
                 yield from vec_candidates(field, logs)
+                yield from cluster_candidates(field, logs)
     if not full:
         two = sorted([s for s in sp if len(s) <= 2], key=lambda s: max(s) - min(s))[:3]
         three = sorted([s for s in sp if len(s) == 3], key=lambda s: max(s) - min(s))[:1]

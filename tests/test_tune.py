@@ -70,9 +70,9 @@ def test_packaged_plans_parse():
                 assert parts[2] in ("b1", "batch")
             # what the library accepts (a rejected entry would make every Context fail)
             assert 1 <= len(e["logs"]) <= 3 and all(1 <= lg <= 13 for lg in e["logs"])
-            assert all((x & ~st.PASS_VEC) in (0, 8, 16, 32) for x in e["E"])
+            assert all((x & ~(st.PASS_VEC | st.PASS_CLUSTER)) in (0, 8, 16, 32) for x in e["E"])
             if any(x & st.PASS_VEC for x in e["E"]):  # the vector-lines build: 8 or 16 points per line
-                assert all((x & ~st.PASS_VEC) in (0, 8, 16) for x in e["E"]), name
+                assert all((x & ~(st.PASS_VEC | st.PASS_CLUSTER)) in (0, 8, 16) for x in e["E"]), name
                 assert len(e["logs"]) > 1, name
             elif 8 in e["E"]:
                 assert all(7 <= lg <= 11 for lg in e["logs"]), name
@@ -89,7 +89,7 @@ def test_plan_candidates_offer_vector_lines_build():
     from stntt_gb300 import tune
 
     cands = list(tune.candidates(st.FIELD_U32, 26, vec=True))
-    vec = [c for c in cands if any(e & st.PASS_VEC for e in c[1])]
+    vec = [c for c in cands if any(e & st.PASS_VEC for e in c[1]) and not any(e & st.PASS_CLUSTER for e in c[1])]
     assert ([9, 9, 8], [8 | st.PASS_VEC, 8 | st.PASS_VEC, 16 | st.PASS_VEC], [32, 32, 32]) in vec
     assert all(len(logs) in (2, 3) and all(7 <= lg <= 10 for lg in logs) and cols[0] in (16, 32)
                for logs, _, cols in vec if max(logs) <= 10)
@@ -99,8 +99,25 @@ def test_plan_candidates_offer_vector_lines_build():
     assert ([13, 13], [16 | st.PASS_VEC] * 2, [8, 8]) not in vec
     assert any(len(logs) == 2 for logs, es, _ in tune.candidates(st.FIELD_GL64, 20, vec=True)
                if any(e & st.PASS_VEC for e in es))
-    gl = [c for c in tune.candidates(st.FIELD_GL64, 24, vec=True) if any(e & st.PASS_VEC for e in c[1])]
+    gl = [c for c in tune.candidates(st.FIELD_GL64, 24, vec=True)
+          if any(e & st.PASS_VEC for e in c[1]) and not any(e & st.PASS_CLUSTER for e in c[1])]
     assert gl and all(cols[0] in (8, 16) for logs, _, cols in gl if max(logs) <= 10)
     assert ([12, 12], [16 | st.PASS_VEC] * 2, [4, 4]) in gl  # two HBM passes at 2^24
     assert not any(logs == [12, 12] and (es[0] & 0xff) == 8 for logs, es, _ in gl)  # 1024 threads
     assert not any(e & st.PASS_VEC for c in tune.candidates(st.FIELD_GL64, 24) for e in c[1])
+
+
+def test_plan_candidates_offer_cluster_passes():
+    """--vec also offers two-pass splits whose 2^11..2^13-point passes run in
+    the vector-lines cluster build (STNTT_PASS_CLUSTER)."""
+    cl = st.PASS_CLUSTER
+    u = [c for c in tune.candidates(st.FIELD_U32, 26, vec=True) if any(e & cl for e in c[1])]
+    assert ([13, 13], [8 | st.PASS_VEC | cl] * 2, [16, 16]) in u
+    assert ([13, 13], [8 | st.PASS_VEC | cl] * 2, [32, 32]) in u  # 1024 threads x 64 registers
+    g = [c for c in tune.candidates(st.FIELD_GL64, 24, vec=True) if any(e & cl for e in c[1])]
+    assert ([12, 12], [8 | st.PASS_VEC | cl] * 2, [8, 8]) in g
+    assert not any(logs == [13, 13] and cols == [16, 16] for logs, _, cols in
+                   (c for c in tune.candidates(st.FIELD_GL64, 26, vec=True) if any(e & cl for e in c[1])))
+    mixed = [c for c in tune.candidates(st.FIELD_GL64, 20, vec=True) if any(e & cl for e in c[1])]
+    assert ([11, 9], [8 | st.PASS_VEC | cl, 8 | st.PASS_VEC], [8, 8]) in mixed
+    assert all(len(logs) == 2 for logs, _, _ in u + g + mixed)
