@@ -13,9 +13,11 @@ Multi-GPU: replicas only (the transform does not shard); every rank runs the
 same workload, value = all ranks' elements / max-over-ranks time.
 
 JSON keys beyond the base contract:
-  e2e           the same metric through the C ABI with host buffers: a pinned
-                copy in, forward + inverse on the caller's stream, a copy out,
-                all inside the timed region
+  e2e           the same metric through the C ABI with host buffers: per step a
+                pinned copy in, forward + inverse on the caller's stream, a copy
+                out, all inside the timed region; steps go round 3 streams with
+                their own buffers (copies of one step overlap another's), and
+                `serial` times them one at a time
   roofline      the dominant kernel (the tile kernel): algorithmic bytes of a
                 transform, B_alg = P_min * 2 * n * w (P_min = 1 when the
                 transform fits one tile, else 2), over the transform time,
@@ -68,6 +70,7 @@ WORKLOADS = {
 DEFAULT_WORKLOAD = "gl64_2^24_fwd+inv"
 METRIC = "NTT Gelem/s (Goldilocks 2^24 forward+inverse, per element transformed)"
 L2_BYTES = 129 * 1024 * 1024
+E2E_SLOTS = 3  # streams (with their own buffers) the end-to-end steps go round
 # largest transform one tile (one HBM pass) holds: 2^12 eight-byte or 2^13 four-byte points
 SINGLE_TILE_LOG = {"gl64": 12, "u32": 13}
 
@@ -781,28 +784,60 @@ def main():
     # End to end through the C ABI: each step copies its input in from pinned
     # host memory, runs forward + inverse (stntt_ntt_gl64 / stntt_ntt_u32 on the
     # caller's stream) and reads the result back, all inside the timed region.
+    # Steps go round E2E_SLOTS streams, each with its own device buffer and
+    # pinned input / output buffers, so one step's copy in overlaps another's
+    # copy out and transform (what a caller streaming data through the GPU
+    # does); `serial` is the same with each step finished before the next.
     e2e = None
     data, ref_copy, fwd, inv, stream = m["data"], m["ref"], m["fwd"], m["inv"], m["stream"]
     if not args.no_e2e:
         dt_host = torch.int64 if field == "gl64" else torch.int32
-        host = torch.empty(n, dtype=dt_host, pin_memory=True)
-        host.copy_(ref_copy.cpu())
+        ref_host = ref_copy.cpu()
         k = max(3, min(args.steps, 50))
+        slots = []
+        for _ in range(E2E_SLOTS):
+            h_in = torch.empty(n, dtype=dt_host, pin_memory=True)
+            h_in.copy_(ref_host)
+            slots.append({"in": h_in, "out": torch.empty(n, dtype=dt_host, pin_memory=True),
+                          "dev": torch.empty(n, dtype=dt_host, device=dev), "stream": torch.cuda.Stream(device=dev)})
+
+        def e2e_step(sl):
+            sp = sl["stream"].cuda_stream
+            with torch.cuda.stream(sl["stream"]):
+                sl["dev"].copy_(sl["in"], non_blocking=True)
+                if field == "gl64":
+                    ctx.ntt_gl64(sl["dev"], lg, 1, inverse=False, stream=sp)
+                    ctx.ntt_gl64(sl["dev"], lg, 1, inverse=True, stream=sp)
+                else:
+                    ctx.ntt_u32(sl["dev"], lg, 1, p_u32, root_u32, inverse=False, stream=sp)
+                    ctx.ntt_u32(sl["dev"], lg, 1, p_u32, root_u32, inverse=True, stream=sp)
+                sl["out"].copy_(sl["dev"], non_blocking=True)
+
+        p_u32, root_u32 = (0, 0) if field == "gl64" else st.params_u32(lg)
+        for sl in slots:  # warm-up: every stream's workspace and the plans exist before timing
+            e2e_step(sl)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        for _ in range(k):
-            with torch.cuda.stream(stream):
-                data.copy_(host, non_blocking=True)
-                fwd()
-                inv()
-                host.copy_(data, non_blocking=True)
-            stream.synchronize()
+        for i in range(k):
+            e2e_step(slots[i % E2E_SLOTS])
+        torch.cuda.synchronize()
         dt = (time.perf_counter() - t0) / k
-        ok = ok and bool(torch.equal(host, ref_copy.cpu()))
+        ok = ok and all(bool(torch.equal(sl["out"], ref_host)) for sl in slots)
+        t0 = time.perf_counter()
+        for _ in range(k):
+            e2e_step(slots[0])
+            slots[0]["stream"].synchronize()
+        dt_serial = (time.perf_counter() - t0) / k
+        ok = ok and bool(torch.equal(slots[0]["out"], ref_host))
         e2e = {"value": world * 2 * n / dt / 1e9, "unit": "Gelem/s", "h2d_bytes_per_step": n * esz,
                "d2h_bytes_per_step": n * esz, "ms_per_step": dt * 1e3,
                "api": ("stntt_ntt_gl64" if field == "gl64" else "stntt_ntt_u32")
-               + " forward then inverse on one stream, pinned copy in before and out after"}
+               + f" forward then inverse per step, pinned copy in before and out after; steps on {E2E_SLOTS} "
+               "streams with their own buffers",
+               "serial": {"value": world * 2 * n / dt_serial / 1e9, "ms_per_step": dt_serial * 1e3,
+                          "api": "the same, each step finished before the next starts"}}
+        host = slots[0]["out"]
+        host.copy_(ref_host)
         if field == "gl64":
             # the host-buffer convenience call, once per direction (each copies in and out)
             hv = host.numpy().view(np.uint64)
@@ -818,7 +853,7 @@ def main():
             e2e["host_call"] = {"value": world * 2 * n / dt2 / 1e9, "ms_per_step": dt2 * 1e3,
                                 "h2d_bytes_per_step": 2 * n * esz, "d2h_bytes_per_step": 2 * n * esz,
                                 "api": "stntt_ntt_gl64_host, forward then inverse (each call copies in and out)"}
-        del host
+        del host, slots
     del m, data, ref_copy
 
     # The other configurations, one GPU only (the replica runs time the headline).

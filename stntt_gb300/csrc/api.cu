@@ -455,7 +455,7 @@ void shape_pass_vec(PassDesc &d, int field, uint64_t col_limit, uint32_t want_E,
     const uint32_t V = field == kFieldGL ? 2 : 4, w = field == kFieldGL ? 8 : 4;
     d.vE = want_E == 8 ? 8 : 16;
     const uint32_t U = (1u << d.logL) / d.vE;
-    const uint32_t gmax = d.logL <= 10 ? 3 : 2, gmin = d.logL <= 10 ? 2 : 1;
+    const uint32_t gmax = d.logL <= 10 ? 3 : 2, gmin = d.logL <= 10 ? 2 : 0;
     const uint32_t tmax = d.logL <= 10 ? 1024 : 512;
     uint32_t logG = gmax;
     for (uint32_t g = gmin; g <= gmax; ++g)
@@ -522,6 +522,14 @@ uint32_t env_log_limit(const char *name, uint32_t dflt) {
 uint32_t full_twiddle_max_log(bool vec) {
     static const uint32_t plain = env_log_limit("STNTT_FULL_TWIDDLE_MAX_LOG", kFullTwiddleMaxLog);
     static const uint32_t v = env_log_limit("STNTT_FULL_TWIDDLE_MAX_LOG_VEC", kFullTwiddleMaxLogVec);
+    return vec ? v : plain;
+}
+// The same for calls of fewer than 2^22 elements: kFullTwiddleMaxLogSmall
+// (plain build) and kFullTwiddleMaxLogSmallVec (vector-lines build), or
+// STNTT_FULL_TWIDDLE_MAX_LOG_SMALL for both.
+uint32_t full_twiddle_max_log_small(bool vec) {
+    static const uint32_t plain = env_log_limit("STNTT_FULL_TWIDDLE_MAX_LOG_SMALL", kFullTwiddleMaxLogSmall);
+    static const uint32_t v = env_log_limit("STNTT_FULL_TWIDDLE_MAX_LOG_SMALL", kFullTwiddleMaxLogSmallVec);
     return vec ? v : plain;
 }
 
@@ -645,7 +653,7 @@ int build_plan(stntt_ctx *ctx, Plan &pl, int field, uint32_t log_n, uint32_t p, 
         // plan. STNTT_FULL_TWIDDLE_MAX_LOG and STNTT_FULL_TWIDDLE_MAX_LOG_VEC
         // (14..26) move the limits of calls of 2^22+ elements.
         if (d.mode == kModeCol && d.logM >= kFullTwiddleMinLog &&
-            d.logM <= (small_call ? kFullTwiddleMaxLogSmall : full_twiddle_max_log(d.vec != 0))) {
+            d.logM <= (small_call ? full_twiddle_max_log_small(d.vec != 0) : full_twiddle_max_log(d.vec != 0))) {
             // Beyond 2^20 points the 32-bit table streams from HBM: there its
             // entries are 4-byte Montgomery values instead of 8-byte Shoup
             // pairs (a 2^26-point table: 256 MiB instead of 512 MiB to read

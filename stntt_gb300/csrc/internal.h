@@ -17,8 +17,12 @@ enum : uint32_t { kModeCol = 0, kModeRow = 1 };  // tile pass kinds (tile.cuh)
 // elements use full tables only up to 2^17 points: a lone 2^20-point call
 // would read its 8 MB table from HBM once per call, as many bytes as its data
 // (measured on GB300, Goldilocks 2^20 forward + inverse with L2 flushed
-// between steps: 84.5 us with the full table, 77.8 us without).
+// between steps: 84.5 us with the full table, 77.8 us without). Passes of
+// small calls in the vector-lines build, whose table loads are 16 bytes wide,
+// take full tables up to 2^21 points (Goldilocks 2^20 forward, best plan:
+// 31.8 us against 32.9; 2^21: 51.4 against 55.4).
 constexpr uint32_t kFullTwiddleMinLog = 14, kFullTwiddleMaxLog = 20, kFullTwiddleMaxLogSmall = 17;
+constexpr uint32_t kFullTwiddleMaxLogSmallVec = 21;
 // Passes in the vector-lines build (tile_v.cuh) of calls of 2^22+ elements
 // use full tables up to 2^26-point sub-problems (see build_plan).
 constexpr uint32_t kFullTwiddleMaxLogVec = 26;

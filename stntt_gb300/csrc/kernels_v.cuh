@@ -73,9 +73,9 @@ cudaError_t launch_v_mode(const PassDesc &d, const TileArgs<F> &a, uint64_t bloc
 
 template <class F, int E, int LOGL>
 cudaError_t launch_v_g(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks, cudaStream_t s) {
-    // line groups per CTA: 4 or 8 up to 2^10-point tiles; 1 or 2 for the wide
-    // tiles of two-pass plans (2^11 and 2^12 points), at most 512 threads (at
-    // 1024 the 64-register limit spills the tile)
+    // line groups per CTA: 4 or 8 up to 2^10-point tiles; 1, 2 or 4 for the
+    // wide tiles of two-pass plans (2^11 and 2^12 points), at most 512 threads
+    // (at 1024 the 64-register limit spills the tile)
     if constexpr (LOGL <= 10) {
         switch (d.vlogG) {
         case 2: return launch_v_mode<F, E, LOGL, 2>(d, a, blocks, s);
@@ -84,6 +84,10 @@ cudaError_t launch_v_g(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks,
         }
     } else {
         switch (d.vlogG) {
+        case 0:
+            if constexpr ((1u << LOGL) / E <= 512)
+                return launch_v_mode<F, E, LOGL, 0>(d, a, blocks, s);
+            return cudaErrorNotSupported;
         case 1:
             if constexpr ((2u << LOGL) / E <= 512)
                 return launch_v_mode<F, E, LOGL, 1>(d, a, blocks, s);
@@ -162,8 +166,9 @@ template <class F, int E>
 cudaError_t preload_v_e() {
     const cudaError_t list[] = {preload_v_lg<F, E, 7, 2>(),  preload_v_lg<F, E, 7, 3>(),  preload_v_lg<F, E, 8, 2>(),
                                 preload_v_lg<F, E, 8, 3>(),  preload_v_lg<F, E, 9, 2>(),  preload_v_lg<F, E, 9, 3>(),
-                                preload_v_lg<F, E, 10, 2>(), preload_v_lg<F, E, 10, 3>(), preload_v_wide<F, E, 11, 1>(),
-                                preload_v_wide<F, E, 11, 2>(), preload_v_wide<F, E, 12, 1>(), preload_v_wide<F, E, 12, 2>()};
+                                preload_v_lg<F, E, 10, 2>(), preload_v_lg<F, E, 10, 3>(), preload_v_wide<F, E, 11, 0>(),
+                                preload_v_wide<F, E, 11, 1>(), preload_v_wide<F, E, 11, 2>(), preload_v_wide<F, E, 12, 0>(),
+                                preload_v_wide<F, E, 12, 1>(),  preload_v_wide<F, E, 12, 2>()};
     for (cudaError_t e : list)
         if (e != cudaSuccess)
             return e;

@@ -50,8 +50,9 @@ def vec_candidates(field: int, logs: list[int]) -> Iterable[tuple[list[int], lis
     passes are 2^7..2^10 points: 8 or 16 points per line per pass, 4 or 8
     line groups per CTA (V = 4 lines per thread for the 32-bit field, 2 for
     Goldilocks); two-pass splits with 2^11 or 2^12-point passes (the wide
-    tiles that reach two HBM passes at 2^22..2^24 points) take 2 or 4 line
-    groups, within 512 threads and 200 KiB of shared memory."""
+    tiles that reach two HBM passes at 2^22..2^24 points, and spread single
+    small transforms over more CTAs) take 1, 2 or 4 line groups, within 512
+    threads and 200 KiB of shared memory."""
     if len(logs) < 2 or not all(7 <= lg <= 12 for lg in logs):
         return
     if len(logs) > 2 and any(lg > 10 for lg in logs):
@@ -60,15 +61,16 @@ def vec_candidates(field: int, logs: list[int]) -> Iterable[tuple[list[int], lis
     w = 8 if field == st.FIELD_GL64 else 4
     wide = any(lg > 10 for lg in logs)
     for es in itertools.product((8 | st.PASS_VEC, 16 | st.PASS_VEC), repeat=len(logs)):
-        for g in ((2, 4) if wide else (4, 8)):  # line groups per CTA
-            ok = True
+        for g in ((1, 2, 4) if wide else (4, 8)):  # line groups per CTA
+            ok, cols = True, []
             for lg, e in zip(logs, es):
                 gg = g if lg > 10 else max(g, 4)
                 threads = gg * (1 << lg) // (e & 0xff)
                 if threads > (512 if lg > 10 else 1024) or gg * v * (1 << lg) * w > 200 * 1024:
                     ok = False
+                cols.append(gg * v)
             if ok:
-                yield list(logs), list(es), [g * v] * len(logs)
+                yield list(logs), list(es), cols
 
 
 def cluster_candidates(field: int, logs: list[int]) -> Iterable[tuple[list[int], list[int], list[int]]]:

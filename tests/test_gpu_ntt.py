@@ -681,6 +681,8 @@ VEC = st.PASS_VEC
     ("gl64", 23, [11, 12], 1, 4),
     ("u32", 22, [11, 11], 1, 16),      # 4 line groups of 2^11 points
     ("u32", 23, [12, 11], 1, 8),
+    ("gl64", 20, [9, 11], 2, 2),       # one line group of 2^11 points (the narrowest, padded)
+    ("u32", 21, [10, 11], 1, 4),
 ])
 def test_vector_lines_build(ctx, field, lg, logs, batch, cols):
     """STNTT_PASS_VEC: every pass in the vector-lines build (V adjacent lines

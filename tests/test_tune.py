@@ -93,9 +93,13 @@ def test_plan_candidates_offer_vector_lines_build():
     assert ([9, 9, 8], [8 | st.PASS_VEC, 8 | st.PASS_VEC, 16 | st.PASS_VEC], [32, 32, 32]) in vec
     assert all(len(logs) in (2, 3) and all(7 <= lg <= 10 for lg in logs) and cols[0] in (16, 32)
                for logs, _, cols in vec if max(logs) <= 10)
-    # wide two-pass tiles (2^11, 2^12 points): 2 or 4 line groups within 512 threads
+    # wide two-pass tiles (2^11, 2^12 points): 1, 2 or 4 line groups within 512 threads
     wide = [c for c in vec if max(c[0]) > 10]
-    assert all(len(logs) == 2 and cols[0] in (8, 16) for logs, _, cols in wide)
+    assert all(len(logs) == 2 and all(c in (4, 8, 16) for c, lg in zip(cols, logs) if lg > 10)
+               for logs, _, cols in wide)
+    wide22 = [c for c in tune.candidates(st.FIELD_U32, 22, vec=True)
+              if any(e & st.PASS_VEC for e in c[1]) and not any(e & st.PASS_CLUSTER for e in c[1]) and max(c[0]) > 10]
+    assert ([11, 11], [8 | st.PASS_VEC] * 2, [4, 4]) in wide22  # one line group: more, narrower CTAs
     assert ([13, 13], [16 | st.PASS_VEC] * 2, [8, 8]) not in vec
     assert any(len(logs) == 2 for logs, es, _ in tune.candidates(st.FIELD_GL64, 20, vec=True)
                if any(e & st.PASS_VEC for e in es))
@@ -103,7 +107,8 @@ def test_plan_candidates_offer_vector_lines_build():
           if any(e & st.PASS_VEC for e in c[1]) and not any(e & st.PASS_CLUSTER for e in c[1])]
     assert gl and all(cols[0] in (8, 16) for logs, _, cols in gl if max(logs) <= 10)
     assert ([12, 12], [16 | st.PASS_VEC] * 2, [4, 4]) in gl  # two HBM passes at 2^24
-    assert not any(logs == [12, 12] and (es[0] & 0xff) == 8 for logs, es, _ in gl)  # 1024 threads
+    # at most 512 threads for the wide tiles: 2^12 points at 8 per line only with one line group
+    assert all(cols[0] == 2 for logs, es, cols in gl if logs == [12, 12] and (es[0] & 0xff) == 8)
     assert not any(e & st.PASS_VEC for c in tune.candidates(st.FIELD_GL64, 24) for e in c[1])
 
 
