@@ -45,6 +45,15 @@ cudaError_t tile_attr() {
 // and 32-bit 2^26 1324 -> 1312 us per step, while replayed graphs of 2^20-point
 // transforms became slower (85 -> 91 us), so smaller calls launch plainly.
 constexpr uint64_t kPdlMinElems = 1ull << 22;
+// kPdlMinElems, or 2^STNTT_PDL_MIN_LOG (0..40) from the environment (read once).
+inline uint64_t pdl_min_elems() {
+    static const uint64_t v = [] {
+        const char *e = getenv("STNTT_PDL_MIN_LOG");
+        const long x = e ? strtol(e, nullptr, 10) : -1;
+        return (x >= 0 && x <= 40) ? (1ull << x) : kPdlMinElems;
+    }();
+    return v;
+}
 
 template <class F, auto KERN>
 cudaError_t launch_tile_k(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks, cudaStream_t s) {
@@ -53,7 +62,7 @@ cudaError_t launch_tile_k(const PassDesc &d, const TileArgs<F> &a, uint64_t bloc
         return e;
     if (d.smem_bytes > 200 * 1024)
         return cudaErrorInvalidConfiguration;
-    if ((a.total << d.logL) < kPdlMinElems) {
+    if ((a.total << d.logL) < pdl_min_elems()) {
         KERN<<<(unsigned)blocks, d.threads, d.smem_bytes, s>>>(a);
         return cudaGetLastError();
     }

@@ -52,8 +52,8 @@ cudaError_t launch_v(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks, c
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
-    // programmatic dependent launch for calls of at least 2^22 elements (see kPdlMinElems)
-    cfg.numAttrs = (a.total << d.logL) >= kPdlMinElems ? 1 : 0;
+    // programmatic dependent launch for calls of at least 2^22 elements (see pdl_min_elems)
+    cfg.numAttrs = (a.total << d.logL) >= pdl_min_elems() ? 1 : 0;
     e = cudaLaunchKernelEx(&cfg, kern, a);
     return e == cudaSuccess ? cudaGetLastError() : e;
 }

@@ -35,8 +35,8 @@ cudaError_t launch_vc(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks, 
     attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     attr[1].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
-    // programmatic dependent launch for calls of at least 2^22 elements (see kPdlMinElems)
-    cfg.numAttrs = (a.total << d.logL) >= kPdlMinElems ? 2 : 1;
+    // programmatic dependent launch for calls of at least 2^22 elements (see pdl_min_elems)
+    cfg.numAttrs = (a.total << d.logL) >= pdl_min_elems() ? 2 : 1;
     e = cudaLaunchKernelEx(&cfg, kern, a);
     return e == cudaSuccess ? cudaGetLastError() : e;
 }

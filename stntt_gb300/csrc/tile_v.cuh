@@ -254,7 +254,9 @@ __device__ __forceinline__ void vsteps(const TileArgs<F> &a, const F &f, typenam
 // SM). Measured on GB300 (32-bit 2^26, Goldilocks 2^24, forward + inverse):
 // E = 16: 128 registers (1.09 ms against 1.30 at 160 and 1.30 at 255);
 // E = 8: 64 for 4-byte values (1.03 ms against 1.20 at 80), 80 for 8-byte
-// ones (0.677 ms against 0.682 at 64).
+// ones (0.677 ms against 0.682 at 64; with the shift-only internal twiddles
+// the full-table and row passes fit 64 registers without spills, and were
+// still slower there: 0.583 against 0.575 ms).
 template <int E, int W>
 constexpr uint32_t vregs() {
     return E == 16 ? 128 : (W == 8 ? 80 : 64);
