@@ -453,7 +453,9 @@ void shape_pass_vec(PassDesc &d, int field, uint64_t col_limit, uint32_t want_E,
     if (d.logL < 7 || d.logL > 12 || d.do_scale || d.logL >= d.logN)
         return;
     const uint32_t V = field == kFieldGL ? 2 : 4, w = field == kFieldGL ? 8 : 4;
-    d.vE = want_E == 8 ? 8 : 16;
+    d.vE = (want_E == 4 || want_E == 8) ? want_E : 16;
+    if (d.vE == 4 && (d.logL < 9 || d.logL > 11))  // 4 points per line: built for 2^9..2^11-point passes
+        return;
     const uint32_t U = (1u << d.logL) / d.vE;
     const uint32_t gmax = d.logL <= 10 ? 3 : 2, gmin = d.logL <= 10 ? 2 : 0;
     const uint32_t tmax = d.logL <= 10 ? 1024 : 512;
@@ -1371,8 +1373,10 @@ int set_plan_for(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t npasses, co
         if (lg == 0 || lg > 13)
             return fail(ctx, STNTT_EINVAL, "set_plan: each pass length must be 2^1..2^13");
         const uint32_t eb = e & ~(STNTT_PASS_VEC | STNTT_PASS_CLUSTER);
-        if ((eb != 0 && eb != 8 && eb != 16 && eb != 32) || ((e & STNTT_PASS_VEC) && eb == 32))
-            return fail(ctx, STNTT_EINVAL, "set_plan: elems must be 0, 8, 16 or 32 (STNTT_PASS_VEC with 0, 8 or 16)");
+        const bool vec_e = (e & STNTT_PASS_VEC) != 0;
+        if (vec_e ? (eb != 0 && eb != 4 && eb != 8 && eb != 16) : (eb != 0 && eb != 8 && eb != 16 && eb != 32))
+            return fail(ctx, STNTT_EINVAL,
+                        "set_plan: elems must be 0, 8, 16 or 32 (STNTT_PASS_VEC with 0, 4, 8 or 16)");
         if ((e & STNTT_PASS_CLUSTER) && (!(e & STNTT_PASS_VEC) || (eb != 0 && eb != 8)))
             return fail(ctx, STNTT_EINVAL, "set_plan: STNTT_PASS_CLUSTER goes with STNTT_PASS_VEC and 8 points per line");
         if (c & (c - 1))

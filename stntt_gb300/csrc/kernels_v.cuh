@@ -71,6 +71,12 @@ cudaError_t launch_v_mode(const PassDesc &d, const TileArgs<F> &a, uint64_t bloc
     return launch_v<F, E, LOGL, LOGG, true, 0>(d, a, blocks, s);
 }
 
+// the thread limit of a (E, LOGL, LOGG) shape: 1024 up to 2^10-point tiles, 512 for wider ones
+template <int E, int LOGL, int LOGG>
+constexpr bool vfits() {
+    return ((1u << LOGG) << LOGL) / E <= (LOGL <= 10 ? 1024u : 512u);
+}
+
 template <class F, int E, int LOGL>
 cudaError_t launch_v_g(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks, cudaStream_t s) {
     // line groups per CTA: 4 or 8 up to 2^10-point tiles; 1, 2 or 4 for the
@@ -78,22 +84,28 @@ cudaError_t launch_v_g(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks,
     // (at 1024 the 64-register limit spills the tile)
     if constexpr (LOGL <= 10) {
         switch (d.vlogG) {
-        case 2: return launch_v_mode<F, E, LOGL, 2>(d, a, blocks, s);
-        case 3: return launch_v_mode<F, E, LOGL, 3>(d, a, blocks, s);
+        case 2:
+            if constexpr (vfits<E, LOGL, 2>())
+                return launch_v_mode<F, E, LOGL, 2>(d, a, blocks, s);
+            return cudaErrorNotSupported;
+        case 3:
+            if constexpr (vfits<E, LOGL, 3>())
+                return launch_v_mode<F, E, LOGL, 3>(d, a, blocks, s);
+            return cudaErrorNotSupported;
         default: return cudaErrorNotSupported;
         }
     } else {
         switch (d.vlogG) {
         case 0:
-            if constexpr ((1u << LOGL) / E <= 512)
+            if constexpr (vfits<E, LOGL, 0>())
                 return launch_v_mode<F, E, LOGL, 0>(d, a, blocks, s);
             return cudaErrorNotSupported;
         case 1:
-            if constexpr ((2u << LOGL) / E <= 512)
+            if constexpr (vfits<E, LOGL, 1>())
                 return launch_v_mode<F, E, LOGL, 1>(d, a, blocks, s);
             return cudaErrorNotSupported;
         case 2:
-            if constexpr ((4u << LOGL) / E <= 512)
+            if constexpr (vfits<E, LOGL, 2>())
                 return launch_v_mode<F, E, LOGL, 2>(d, a, blocks, s);
             return cudaErrorNotSupported;
         default: return cudaErrorNotSupported;
@@ -103,14 +115,23 @@ cudaError_t launch_v_g(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks,
 
 template <class F, int E>
 cudaError_t launch_v_l(const PassDesc &d, const TileArgs<F> &a, uint64_t blocks, cudaStream_t s) {
-    switch (d.logL) {
-    case 7: return launch_v_g<F, E, 7>(d, a, blocks, s);
-    case 8: return launch_v_g<F, E, 8>(d, a, blocks, s);
-    case 9: return launch_v_g<F, E, 9>(d, a, blocks, s);
-    case 10: return launch_v_g<F, E, 10>(d, a, blocks, s);
-    case 11: return launch_v_g<F, E, 11>(d, a, blocks, s);
-    case 12: return launch_v_g<F, E, 12>(d, a, blocks, s);
-    default: return cudaErrorNotSupported;
+    if constexpr (E == 4) {  // 4 points per line: the passes of single 2^18..2^22-point calls
+        switch (d.logL) {
+        case 9: return launch_v_g<F, E, 9>(d, a, blocks, s);
+        case 10: return launch_v_g<F, E, 10>(d, a, blocks, s);
+        case 11: return launch_v_g<F, E, 11>(d, a, blocks, s);
+        default: return cudaErrorNotSupported;
+        }
+    } else {
+        switch (d.logL) {
+        case 7: return launch_v_g<F, E, 7>(d, a, blocks, s);
+        case 8: return launch_v_g<F, E, 8>(d, a, blocks, s);
+        case 9: return launch_v_g<F, E, 9>(d, a, blocks, s);
+        case 10: return launch_v_g<F, E, 10>(d, a, blocks, s);
+        case 11: return launch_v_g<F, E, 11>(d, a, blocks, s);
+        case 12: return launch_v_g<F, E, 12>(d, a, blocks, s);
+        default: return cudaErrorNotSupported;
+        }
     }
 }
 
@@ -120,7 +141,7 @@ template <class F>
 cudaError_t launch_tile_vec_t(const PassDesc &d, uint32_t p, const void *tables, const void *in, void *out,
                               uint64_t batch, cudaStream_t s) {
     constexpr uint32_t V = vlines<F>();
-    if (!d.vec || d.vec != V || (d.vE != 8 && d.vE != 16) || d.do_scale || d.logL >= d.logN || !aligned16(in) ||
+    if (!d.vec || d.vec != V || (d.vE != 4 && d.vE != 8 && d.vE != 16) || d.do_scale || d.logL >= d.logN || !aligned16(in) ||
         !aligned16(out) || !aligned16(tables))
         return cudaErrorNotSupported;
     const uint32_t C = V << d.vlogG;
@@ -137,11 +158,15 @@ cudaError_t launch_tile_vec_t(const PassDesc &d, uint32_t p, const void *tables,
         return cudaSuccess;
     if (blocks > 0x7fffffffull)
         return cudaErrorInvalidConfiguration;
-    return d.vE == 8 ? launch_v_l<F, 8>(d, a, blocks, s) : launch_v_l<F, 16>(d, a, blocks, s);
+    return d.vE == 4   ? launch_v_l<F, 4>(d, a, blocks, s)
+           : d.vE == 8 ? launch_v_l<F, 8>(d, a, blocks, s)
+                       : launch_v_l<F, 16>(d, a, blocks, s);
 }
 
 template <class F, int E, int LOGL, int LOGG>
 cudaError_t preload_v_lg() {
+    if constexpr (!vfits<E, LOGL, LOGG>())
+        return cudaSuccess;  // a shape launch_v_g never launches
     cudaError_t e = vattr<F, tile_kernel_v<F, vlines<F>(), E, LOGL, LOGG, false, 0>>();
     if (e == cudaSuccess)
         e = vattr<F, tile_kernel_v<F, vlines<F>(), E, LOGL, LOGG, true, 0>>();
@@ -157,9 +182,7 @@ cudaError_t preload_v_lg() {
 // the wide-tile shapes launch_v_g / launch_tile_vec_t can pick (else nothing to load)
 template <class F, int E, int LOGL, int LOGG>
 cudaError_t preload_v_wide() {
-    if constexpr (((1u << LOGG) << LOGL) / E <= 512)
-        return preload_v_lg<F, E, LOGL, LOGG>();
-    return cudaSuccess;
+    return preload_v_lg<F, E, LOGL, LOGG>();
 }
 
 template <class F, int E>
@@ -177,8 +200,12 @@ cudaError_t preload_v_e() {
 
 template <class F>
 cudaError_t preload_v_t() {
-    const cudaError_t e = preload_v_e<F, 16>();
-    return e == cudaSuccess ? preload_v_e<F, 8>() : e;
+    const cudaError_t list[] = {preload_v_e<F, 16>(),        preload_v_e<F, 8>(),         preload_v_lg<F, 4, 9, 2>(),
+                                preload_v_lg<F, 4, 9, 3>(),  preload_v_lg<F, 4, 10, 2>(), preload_v_wide<F, 4, 11, 0>()};
+    for (cudaError_t e : list)
+        if (e != cudaSuccess)
+            return e;
+    return cudaSuccess;
 }
 
 }  // namespace vlaunch

@@ -228,12 +228,13 @@ __device__ __forceinline__ void vstep(const TileArgs<F> &a, const F &f, typename
 }
 
 // Steps S.. of the tile: one leading radix-2^(LOGL mod log2 E) step when
-// needed, then radix-E steps (E = 16, or 8 for half the registers).
+// needed, then radix-E steps (E = 16, or 8 for half the registers, or 4 for
+// twice the threads of single small transforms).
 template <class F, int V, int E, int LOGL, int LOGG, int S, bool COL, int FULL4>
 __device__ __forceinline__ void vsteps(const TileArgs<F> &a, const F &f, typename F::T (&x)[V][E],
                                        typename F::T *sm_g, uint32_t u, const VGeo<typename F::T, V> &geo) {
-    static_assert(E == 8 || E == 16, "radix-8 or radix-16 steps");
-    constexpr int LE = E == 8 ? 3 : 4;
+    static_assert(E == 4 || E == 8 || E == 16, "radix-4, radix-8 or radix-16 steps");
+    constexpr int LE = E == 4 ? 2 : E == 8 ? 3 : 4;
     constexpr int TAIL = LOGL % LE;
     constexpr int NS = LOGL / LE + (TAIL > 0 ? 1 : 0);
     if constexpr (S < NS) {

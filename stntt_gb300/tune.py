@@ -47,7 +47,8 @@ def splits(log_n: int, max_pass: int = 13) -> list[list[int]]:
 
 def vec_candidates(field: int, logs: list[int]) -> Iterable[tuple[list[int], list[int], list[int]]]:
     """The vector-lines build (STNTT_PASS_VEC) of a multi-pass split whose
-    passes are 2^7..2^10 points: 8 or 16 points per line per pass, 4 or 8
+    passes are 2^7..2^10 points: 8 or 16 points per line per pass (also 4
+    where every pass is 2^9..2^11 points), 4 or 8
     line groups per CTA (V = 4 lines per thread for the 32-bit field, 2 for
     Goldilocks); two-pass splits with 2^11 or 2^12-point passes (the wide
     tiles that reach two HBM passes at 2^22..2^24 points, and spread single
@@ -60,7 +61,10 @@ def vec_candidates(field: int, logs: list[int]) -> Iterable[tuple[list[int], lis
     v = 2 if field == st.FIELD_GL64 else 4
     w = 8 if field == st.FIELD_GL64 else 4
     wide = any(lg > 10 for lg in logs)
-    for es in itertools.product((8 | st.PASS_VEC, 16 | st.PASS_VEC), repeat=len(logs)):
+    per_line = (8 | st.PASS_VEC, 16 | st.PASS_VEC)
+    if all(9 <= lg <= 11 for lg in logs):
+        per_line += (4 | st.PASS_VEC,)  # twice the threads: for single transforms too small to fill the SMs
+    for es in itertools.product(per_line, repeat=len(logs)):
         for g in ((1, 2, 4) if wide else (4, 8)):  # line groups per CTA
             ok, cols = True, []
             for lg, e in zip(logs, es):

@@ -920,3 +920,30 @@ def test_vector_lines_cluster_pass_full_size(ctx, field, lg, logs, cols):
         ctx.clear_plans()
         from stntt_gb300 import tune
         tune.apply_cache(ctx)
+
+
+@pytest.mark.parametrize("field,lg,logs,cols", [("gl64", 20, [11, 9], [2, 8]), ("gl64", 18, [9, 9], [16, 8]),
+                                                ("u32", 20, [9, 11], [16, 4]), ("u32", 21, [10, 11], [16, 4])])
+def test_vector_lines_four_points_per_line(ctx, field, lg, logs, cols):
+    """4 points per line (radix-4 steps, twice the threads): the passes of
+    single small transforms, forward and inverse against the oracle."""
+    fid = st.FIELD_GL64 if field == "gl64" else st.FIELD_U32
+    try:
+        ctx.set_plan(fid, lg, logs, elems=[4 | VEC] * len(logs), cols=cols)
+        n = 1 << lg
+        for inv in (False, True):
+            if field == "gl64":
+                x = O.uniform_u64(600 + lg, n)
+                d = dev64(x)
+                ctx.ntt_gl64(d, lg, 1, inverse=inv)
+                assert np.array_equal(host64(d), O.ntt_gl64(x, inverse=inv, threads=8)), inv
+            else:
+                p, root = st.params_u32(lg)
+                x = O.uniform_u32(600 + lg, p, n)
+                d = dev32(x)
+                ctx.ntt_u32(d, lg, 1, p, root, inverse=inv)
+                assert np.array_equal(host32(d), O.ntt_u32(x, root, p, inverse=inv, threads=8)), inv
+    finally:
+        ctx.clear_plans()
+        from stntt_gb300 import tune
+        tune.apply_cache(ctx)

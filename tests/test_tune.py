@@ -70,9 +70,9 @@ def test_packaged_plans_parse():
                 assert parts[2] in ("b1", "batch")
             # what the library accepts (a rejected entry would make every Context fail)
             assert 1 <= len(e["logs"]) <= 3 and all(1 <= lg <= 13 for lg in e["logs"])
-            assert all((x & ~(st.PASS_VEC | st.PASS_CLUSTER)) in (0, 8, 16, 32) for x in e["E"])
+            assert all((x & ~(st.PASS_VEC | st.PASS_CLUSTER)) in (0, 4, 8, 16, 32) for x in e["E"])
             if any(x & st.PASS_VEC for x in e["E"]):  # the vector-lines build: 8 or 16 points per line
-                assert all((x & ~(st.PASS_VEC | st.PASS_CLUSTER)) in (0, 8, 16) for x in e["E"]), name
+                assert all((x & ~(st.PASS_VEC | st.PASS_CLUSTER)) in (0, 4, 8, 16) for x in e["E"]), name
                 assert len(e["logs"]) > 1, name
             elif 8 in e["E"]:
                 assert all(7 <= lg <= 11 for lg in e["logs"]), name
