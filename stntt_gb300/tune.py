@@ -141,20 +141,33 @@ def candidates(field: int, log_n: int, full: bool = False,
 def _time_plan(ctx: st.Context, field: int, log_n: int, data, p: int, root: int, batch: int, reps: int,
                flush) -> float:
     """Mean device time of one forward call (CUDA events around each call),
-    with L2 flushed before every call as in bench.py."""
+    with L2 flushed before every call as in bench.py. Calls of fewer than 2^22
+    elements are captured once as a CUDA graph and replayed, as bench.py times
+    them (a direct call's host work can leave gaps between its kernels)."""
     import torch
 
-    run = (lambda: ctx.ntt_gl64(data, log_n, batch)) if field == st.FIELD_GL64 else \
-        (lambda: ctx.ntt_u32(data, log_n, batch, p, root))
-    run()
-    torch.cuda.synchronize()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
-    for a, b in ev:
-        flush.zero_()
-        a.record()
+    stream = torch.cuda.Stream(device=data.device)
+    sp = stream.cuda_stream
+    run = (lambda: ctx.ntt_gl64(data, log_n, batch, stream=sp)) if field == st.FIELD_GL64 else \
+        (lambda: ctx.ntt_u32(data, log_n, batch, p, root, stream=sp))
+    with torch.cuda.stream(stream):
         run()
-        b.record()
-    torch.cuda.synchronize()
+        stream.synchronize()
+        if (batch << log_n) < (1 << 22):
+            graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(graph, stream=stream, capture_error_mode="relaxed"):
+                run()
+            step = graph.replay
+        else:
+            step = run
+        step()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+        for a, b in ev:
+            flush.zero_()
+            a.record(stream)
+            step()
+            b.record(stream)
+        torch.cuda.synchronize()
     return sum(a.elapsed_time(b) for a, b in ev) * 1e3 / reps  # microseconds per call
 
 
