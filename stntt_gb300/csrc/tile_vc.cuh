@@ -36,17 +36,14 @@ __device__ __forceinline__ uint32_t vc_rank() {
     return r;
 }
 
-// Every thread of every CTA of the cluster; orders shared-memory accesses
-// across the cluster (release / acquire). The arrive and the wait may be
-// apart: work between them overlaps the other CTAs' arrival.
+// The cluster barrier, for every thread of every CTA of the cluster; it
+// orders shared-memory accesses across the cluster (release on arrive,
+// acquire on wait). Work between the arrive and the wait overlaps the other
+// CTAs' arrival.
 __device__ __forceinline__ void vc_cluster_arrive() {
     asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
 }
 __device__ __forceinline__ void vc_cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
-__device__ __forceinline__ void vc_cluster_sync() {
-    vc_cluster_arrive();
-    vc_cluster_wait();
-}
 
 // 16 bytes (V elements) from CTA `rank`'s shared memory at the offset of the
 // local address p.
@@ -73,7 +70,8 @@ __device__ __forceinline__ void v16_load_cluster(T (&x)[V], const T *p, uint32_t
 // tile (see vstep in tile_v.cuh). The step twiddles w_(L_S)^e come from the
 // pass's w_L table at e << TWS. FIRST reads through load(idx, t), LAST writes
 // through store(pos, v), the others use the shared-memory tile. SYNC between
-// this step's reads and its writes: 0 none, 1 the CTA, 2 the cluster.
+// this step's reads and its writes: 0 none, 1 the CTA, 2 the cluster (its
+// arrive right after the reads, its wait before the writes).
 template <class F, int V, int E, int LOGS, int LOGGT, int LOGR, int LOGP, int TWS, bool FIRST, bool LAST, int SYNC,
           class LOAD, class STORE>
 __device__ __forceinline__ void vcstep(const TileArgs<F> &a, const F &f, typename F::T (&x)[V][E],
