@@ -1921,6 +1921,16 @@ void args_fill(int field, const PassDesc &d, uint32_t p, const void *t, const un
 
 // 512-thread tile shape for the persistent kernel: 16 elements per thread,
 // C = 8192 / L columns or rows.
+// Goldilocks items of two-pass jobs in the vector-lines layout: on unless
+// STNTT_BATCH_VEC=0 (read once).
+bool batch_vec_items() {
+    static const bool v = [] {
+        const char *e = getenv("STNTT_BATCH_VEC");
+        return !(e && e[0] == '0');
+    }();
+    return v;
+}
+
 void batch_shape(PassDesc &d, int field) {
     const uint32_t L = 1u << d.logL;
     d.E = 16;
@@ -2013,6 +2023,18 @@ int build_part(stntt_ctx *ctx, stntt_batch *bt, int field, const std::vector<con
             batch_shape(d0, field);
             batch_shape(d1, field);
             smem = std::max({smem, d0.smem_bytes, d1.smem_bytes});
+            // Goldilocks: the items run the vector-lines steps (batch_item_vec)
+            // when every job's data is 16-byte aligned, both passes are
+            // 2^4..2^11 points and the column pass has a full four-step table
+            // (and 16-byte aligned: an even entry offset from the 256-byte aligned table allocation)
+            bool vec = field == kFieldGL && batch_vec_items() && d0.full_off != ~0ull && (d0.full_off & 1u) == 0 &&
+                       !d0.full_mont && d0.logL >= 4 && d0.logL <= 11 && d1.logL >= 4 && d1.logL <= 11;
+            for (const stntt_job *j : cj)
+                vec = vec && ((uintptr_t)j->data & 15u) == 0;
+            if (vec) {
+                d0.vec = d1.vec = 2;
+                smem = std::max({smem, vec_smem(2, 12 - d0.logL, d0.logL, 8), vec_smem(2, 12 - d1.logL, d1.logL, 8)});
+            }
             const uint32_t a0 = (uint32_t)pend.size();
             pend.push_back({d0, ck.p, pl->d_tables, data_off, scr_off, (uint64_t)J << (ck.log_n - d0.logL)});
             const uint32_t a1 = (uint32_t)pend.size();

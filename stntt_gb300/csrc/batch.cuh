@@ -18,7 +18,7 @@
 #include <cstring>
 #include <type_traits>
 
-#include "tile.cuh"
+#include "tile_v.cuh"
 
 namespace stntt {
 
@@ -63,9 +63,77 @@ __device__ __noinline__ void batch_item_small(const TileArgs<F> &sa, uint64_t bl
     }
 }
 
-// One item of any tile length (every item: 16 elements per thread).
+// A Goldilocks item of a two-pass job in the vector-lines layout (tile_v.cuh):
+// C = 2^(13 - LOGL) lines of one job, two adjacent lines and 8 points per
+// thread (512 threads), 16-byte HBM accesses; a column item carries its
+// four-step twiddle in a full table. Geometry as in tile_kernel_v, with the
+// job's data reached through the item's pointer arrays.
+template <class F, int LOGL, bool COL>
+__device__ __noinline__ void batch_item_vec(const TileArgs<F> &a, uint64_t blk, typename F::T *sm) {
+    using T = typename F::T;
+    constexpr int V = 2, E = 8, LOGG = 12 - LOGL;
+    static_assert(LOGG >= 0 && (1u << LOGG) * ((1u << LOGL) / E) == kBatchThreads, "512 threads per item");
+    constexpr uint32_t G = 1u << LOGG, C = V * G;
+    const uint32_t g = threadIdx.x & (G - 1), u = threadIdx.x >> LOGG;
+    F f;
+    f.p = a.p;
+    const uint64_t line0 = blk * C + g * V;
+    const uint32_t logPer = a.logN - LOGL;
+    const uint64_t b = line0 >> logPer, rem = line0 & ((1ull << logPer) - 1);
+    const T *ibase = reinterpret_cast<const T *>(a.in_ptrs[b]);
+    T *obase = reinterpret_cast<T *>(a.out_ptrs[b]);
+    VGeo<T, V> geo;
+    if constexpr (COL) {
+        const uint64_t q = rem >> a.logS;
+        geo.col0 = (uint32_t)(rem & ((1ull << a.logS) - 1));
+        geo.src[0] = ibase + (q << a.logM) + geo.col0;
+        geo.src[1] = geo.src[0];
+        geo.dst = obase + (q << a.logM) + geo.col0;
+        geo.istride = geo.ostride = 1u << a.logS;
+    } else {
+#pragma unroll
+        for (int i = 0; i < V; ++i) {
+            const uint64_t r = rem + i;
+            const uint64_t inrow = ((r & ((1ull << a.logN1) - 1)) << a.logN2) + (r >> a.logN1);
+            geo.src[i] = ibase + (inrow << LOGL);
+        }
+        geo.dst = obase + rem;
+        geo.istride = 1;
+        geo.ostride = 1u << logPer;
+        geo.col0 = 0;
+    }
+    T x[V][E];
+    vsteps<F, V, E, LOGL, LOGG, 0, COL, COL ? 1 : 0>(a, f, x, sm + g * V, u, geo);
+}
+
+template <class F, bool COL>
+__device__ __forceinline__ void batch_item_vec_l(const TileArgs<F> &sa, uint64_t blk, typename F::T *sm) {
+    switch (sa.logL) {
+    case 4: batch_item_vec<F, 4, COL>(sa, blk, sm); break;
+    case 5: batch_item_vec<F, 5, COL>(sa, blk, sm); break;
+    case 6: batch_item_vec<F, 6, COL>(sa, blk, sm); break;
+    case 7: batch_item_vec<F, 7, COL>(sa, blk, sm); break;
+    case 8: batch_item_vec<F, 8, COL>(sa, blk, sm); break;
+    case 9: batch_item_vec<F, 9, COL>(sa, blk, sm); break;
+    case 10: batch_item_vec<F, 10, COL>(sa, blk, sm); break;
+    case 11: batch_item_vec<F, 11, COL>(sa, blk, sm); break;
+    default: break;  // the host sets vecl only for 2^4..2^11-point passes
+    }
+}
+
+// One item of any tile length (every item: 16 elements per thread, or the
+// vector-lines layout where the host marked the pass).
 template <class F>
 __device__ __forceinline__ void batch_item(const TileArgs<F> &sa, uint64_t blk, typename F::T *sm) {
+    if constexpr (IsPow2Field<F>::value) {
+        if (sa.vecl == 2) {
+            if (sa.mode == kModeCol)
+                batch_item_vec_l<F, true>(sa, blk, sm);
+            else
+                batch_item_vec_l<F, false>(sa, blk, sm);
+            return;
+        }
+    }
     switch (sa.logL) {
     case 4: batch_item_l<F, 4>(sa, blk, sm); break;
     case 5: batch_item_l<F, 5>(sa, blk, sm); break;

@@ -217,6 +217,7 @@ void fill_args(TileArgs<F> &a, const PassDesc &d, uint32_t p, const void *tables
     a.tw4_mont = (d.full_off != ~0ull && d.full_mont) ? reinterpret_cast<const uint32_t *>(tab + d.full_off) : nullptr;
     a.pinv = d.pinv;
     a.pow2 = d.pow2;
+    a.vecl = d.vec;
     for (int j = 0; j < 8; ++j)
         std::memcpy(&a.wR[j], &d.wR[j], sizeof(TW));
     std::memcpy(&a.scale, &d.scale, sizeof(TW));

@@ -72,6 +72,10 @@ struct TileArgs {
     // Goldilocks: PassDesc::pow2 (1 forward root, 2 inverse root, 0 other);
     // the batched kernel picks the direction-specialised field type by it.
     uint32_t pow2;
+    // Batched launch: 2 when this pass's items run the vector-lines steps
+    // (two lines per thread, 16-byte accesses; every job pointer 16-byte
+    // aligned), else 0.
+    uint32_t vecl;
 };
 
 template <class F>
