@@ -1964,8 +1964,12 @@ struct ClassKey {
 int build_part(stntt_ctx *ctx, stntt_batch *bt, int field, const std::vector<const stntt_job *> &jobs,
                size_t &scratch_cursor) {
     std::map<ClassKey, std::vector<const stntt_job *>> classes;
-    for (const stntt_job *j : jobs)
+    bool lazy = field == kFieldU32;  // the part's kernel: the lazy 32-bit field when every p < 2^30
+    for (const stntt_job *j : jobs) {
         classes[{j->log_n, j->dir, field == kFieldGL ? 0u : j->p, field == kFieldGL ? 0u : j->root}].push_back(j);
+        if (field == kFieldU32 && j->p >= (1u << 30))
+            lazy = false;
+    }
     const size_t asz = args_size(field);
     std::vector<unsigned char> args;                   // TileArgs, by value
     std::vector<unsigned long long> ptrs;              // per-class data / scratch pointer arrays
@@ -2023,17 +2027,23 @@ int build_part(stntt_ctx *ctx, stntt_batch *bt, int field, const std::vector<con
             batch_shape(d0, field);
             batch_shape(d1, field);
             smem = std::max({smem, d0.smem_bytes, d1.smem_bytes});
-            // Goldilocks: the items run the vector-lines steps (batch_item_vec)
-            // when every job's data is 16-byte aligned, both passes are
-            // 2^4..2^11 points and the column pass has a full four-step table
-            // (and 16-byte aligned: an even entry offset from the 256-byte aligned table allocation)
-            bool vec = field == kFieldGL && batch_vec_items() && d0.full_off != ~0ull && (d0.full_off & 1u) == 0 &&
-                       !d0.full_mont && d0.logL >= 4 && d0.logL <= 11 && d1.logL >= 4 && d1.logL <= 11;
+            // The items run the vector-lines steps (batch_item_vec) when every
+            // job's data is 16-byte aligned, both passes are 2^4..2^11 points
+            // and the column pass has a full four-step table (16-byte aligned:
+            // an even entry offset from the 256-byte aligned table
+            // allocation); for the 32-bit field only in a part of the lazy
+            // field (every p < 2^30), whose kernel has these steps.
+            const uint32_t V = field == kFieldGL ? 2 : 4, w = field == kFieldGL ? 8 : 4;
+            bool vec = (field == kFieldGL || lazy) && batch_vec_items() && d0.full_off != ~0ull &&
+                       (d0.full_off & 1u) == 0 && !d0.full_mont && d0.logL >= 4 && d0.logL <= 11 && d1.logL >= 4 &&
+                       d1.logL <= 11;
             for (const stntt_job *j : cj)
                 vec = vec && ((uintptr_t)j->data & 15u) == 0;
             if (vec) {
-                d0.vec = d1.vec = 2;
-                smem = std::max({smem, vec_smem(2, 12 - d0.logL, d0.logL, 8), vec_smem(2, 12 - d1.logL, d1.logL, 8)});
+                d0.vec = d1.vec = V;
+                const uint32_t lv = V == 2 ? 1 : 2;
+                smem = std::max({smem, vec_smem(V, 13 - d0.logL - lv, d0.logL, w),
+                                 vec_smem(V, 13 - d1.logL - lv, d1.logL, w)});
             }
             const uint32_t a0 = (uint32_t)pend.size();
             pend.push_back({d0, ck.p, pl->d_tables, data_off, scr_off, (uint64_t)J << (ck.log_n - d0.logL)});
@@ -2052,10 +2062,7 @@ int build_part(stntt_ctx *ctx, stntt_batch *bt, int field, const std::vector<con
     }
     BatchPart part;
     part.field = field;
-    part.lazy = field == kFieldU32;
-    for (const stntt_job *j : jobs)
-        if (field == kFieldU32 && j->p >= (1u << 30))
-            part.lazy = false;
+    part.lazy = lazy;
     part.nitems = phaseA.size() + phaseB.size();
     part.ncounters = std::max<uint32_t>(njob2, 1);
     part.smem = smem;

@@ -63,15 +63,21 @@ __device__ __noinline__ void batch_item_small(const TileArgs<F> &sa, uint64_t bl
     }
 }
 
-// A Goldilocks item of a two-pass job in the vector-lines layout (tile_v.cuh):
-// C = 2^(13 - LOGL) lines of one job, two adjacent lines and 8 points per
-// thread (512 threads), 16-byte HBM accesses; a column item carries its
-// four-step twiddle in a full table. Geometry as in tile_kernel_v, with the
-// job's data reached through the item's pointer arrays.
+// An item of a two-pass job in the vector-lines layout (tile_v.cuh): C =
+// 8192 / L lines of one job, V adjacent lines per thread (16 bytes: two
+// Goldilocks values with 8 points each, or four 32-bit values with 4 points
+// each, so 512 threads either way), 16-byte HBM accesses; a column item
+// carries its four-step twiddle in a full table. Geometry as in
+// tile_kernel_v, with the job's data reached through the item's pointer
+// arrays.
+template <class F>
+__host__ __device__ constexpr int batch_vlines() {
+    return sizeof(typename F::T) == 8 ? 2 : 4;
+}
 template <class F, int LOGL, bool COL>
 __device__ __noinline__ void batch_item_vec(const TileArgs<F> &a, uint64_t blk, typename F::T *sm) {
     using T = typename F::T;
-    constexpr int V = 2, E = 8, LOGG = 12 - LOGL;
+    constexpr int V = batch_vlines<F>(), E = 16 / V, LOGG = 13 - LOGL - (V == 2 ? 1 : 2);
     static_assert(LOGG >= 0 && (1u << LOGG) * ((1u << LOGL) / E) == kBatchThreads, "512 threads per item");
     constexpr uint32_t G = 1u << LOGG, C = V * G;
     const uint32_t g = threadIdx.x & (G - 1), u = threadIdx.x >> LOGG;
@@ -87,7 +93,9 @@ __device__ __noinline__ void batch_item_vec(const TileArgs<F> &a, uint64_t blk, 
         const uint64_t q = rem >> a.logS;
         geo.col0 = (uint32_t)(rem & ((1ull << a.logS) - 1));
         geo.src[0] = ibase + (q << a.logM) + geo.col0;
-        geo.src[1] = geo.src[0];
+#pragma unroll
+        for (int i = 1; i < V; ++i)
+            geo.src[i] = geo.src[0];
         geo.dst = obase + (q << a.logM) + geo.col0;
         geo.istride = geo.ostride = 1u << a.logS;
     } else {
@@ -121,12 +129,17 @@ __device__ __forceinline__ void batch_item_vec_l(const TileArgs<F> &sa, uint64_t
     }
 }
 
+template <class F>
+__host__ __device__ constexpr bool batch_vec_field() {
+    return IsPow2Field<F>::value || std::is_same_v<F, FieldU32L>;
+}
+
 // One item of any tile length (every item: 16 elements per thread, or the
 // vector-lines layout where the host marked the pass).
 template <class F>
 __device__ __forceinline__ void batch_item(const TileArgs<F> &sa, uint64_t blk, typename F::T *sm) {
-    if constexpr (IsPow2Field<F>::value) {
-        if (sa.vecl == 2) {
+    if constexpr (batch_vec_field<F>()) {
+        if (sa.vecl == (uint32_t)batch_vlines<F>()) {
             if (sa.mode == kModeCol)
                 batch_item_vec_l<F, true>(sa, blk, sm);
             else

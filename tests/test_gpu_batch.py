@@ -182,27 +182,45 @@ def test_full_reference_mix_matches_per_call(ctx):
     del data, ref
 
 
-def test_batch_vector_lines_items_and_unaligned_fallback(ctx):
-    """Goldilocks two-pass jobs run their items in the vector-lines layout when
-    every job of their class is 16-byte aligned; a class with a job 8 bytes
-    off falls back to the 16-points-per-thread items. Both against the
-    oracle, both directions."""
+@pytest.mark.parametrize("field", ["gl64", "u32"])
+def test_batch_vector_lines_items_and_unaligned_fallback(ctx, field):
+    """Two-pass jobs run their items in the vector-lines layout when every job
+    of their class is 16-byte aligned; a class with a job off 16-byte
+    alignment falls back to the 16-points-per-thread items. Both against the
+    oracle, both directions, both fields."""
     sizes = [14, 14, 15, 15, 17, 18]
-    offs = [0, 0, 0, 1, 0, 0]  # the 2^15 class gets one job 8 bytes off 16-byte alignment
-    total = sum((1 << s) + 2 for s in sizes)
-    buf = torch.zeros(total, dtype=torch.int64, device="cuda")
-    jobs, views, inputs = [], [], []
+    offs = [0, 0, 0, 1, 0, 0]  # the 2^15 class gets one job off 16-byte alignment
+    w = 8 if field == "gl64" else 4
+    step = 16 // w
+    total = sum((1 << s) + step for s in sizes)
+    dt = torch.int64 if field == "gl64" else torch.int32
+    buf = torch.zeros(total, dtype=dt, device="cuda")
+    jobs, views, inputs, params = [], [], [], []
     pos = 0
     for i, (s, o) in enumerate(zip(sizes, offs)):
-        x = O.uniform_u64(4242 + i, 1 << s)
+        if field == "gl64":
+            x = O.uniform_u64(4242 + i, 1 << s)
+            src = torch.from_numpy(x.view(np.int64))
+            p = root = 0
+        else:
+            p, root = st.params_u32(s)
+            x = O.uniform_u32(4242 + i, p, 1 << s)
+            src = torch.from_numpy(x.view(np.int32))
         v = buf[pos + o: pos + o + (1 << s)]
-        v.copy_(torch.from_numpy(x.view(np.int64)))
-        jobs.append(st.Job(st.FIELD_GL64, s, i % 2, 0, 0, 0, v.data_ptr()))
+        v.copy_(src)
+        jobs.append(st.Job(st.FIELD_GL64 if field == "gl64" else st.FIELD_U32, s, i % 2, p, root, 0, v.data_ptr()))
         views.append(v)
         inputs.append(x)
-        pos += (1 << s) + 2
-    assert views[3].data_ptr() % 16 == 8 and views[2].data_ptr() % 16 == 0
+        params.append((p, root))
+        pos += (1 << s) + step
+    assert views[3].data_ptr() % 16 != 0 and views[2].data_ptr() % 16 == 0
     ctx.ntt_batch(jobs)
     torch.cuda.synchronize()
-    for i, (v, x) in enumerate(zip(views, inputs)):
-        assert np.array_equal(v.cpu().numpy().view(np.uint64), O.ntt_gl64(x, inverse=bool(i % 2))), sizes[i]
+    for i, (v, x, (p, root)) in enumerate(zip(views, inputs, params)):
+        if field == "gl64":
+            want = O.ntt_gl64(x, inverse=bool(i % 2))
+            got = v.cpu().numpy().view(np.uint64)
+        else:
+            want = O.ntt_u32(x, root, p, inverse=bool(i % 2))
+            got = v.cpu().numpy().view(np.uint32)
+        assert np.array_equal(got, want), (field, sizes[i])
