@@ -15,7 +15,7 @@ same workload, value = all ranks' elements / max-over-ranks time.
 JSON keys beyond the base contract:
   e2e           the same metric through the C ABI with host buffers: per step a
                 pinned copy in, forward + inverse on the caller's stream, a copy
-                out, all inside the timed region; steps go round 3 streams with
+                out, all inside the timed region; steps go round 4 streams with
                 their own buffers (copies of one step overlap another's), and
                 `serial` times them one at a time
   roofline      the dominant kernel (the tile kernel): algorithmic bytes of a
@@ -70,7 +70,7 @@ WORKLOADS = {
 DEFAULT_WORKLOAD = "gl64_2^24_fwd+inv"
 METRIC = "NTT Gelem/s (Goldilocks 2^24 forward+inverse, per element transformed)"
 L2_BYTES = 129 * 1024 * 1024
-E2E_SLOTS = 3  # streams (with their own buffers) the end-to-end steps go round
+E2E_SLOTS = 4  # streams (with their own buffers) the end-to-end steps go round (2: 31.4, 3: 38.3, 4: 39.6 Gelem/s)
 # largest transform one tile (one HBM pass) holds: 2^12 eight-byte or 2^13 four-byte points
 SINGLE_TILE_LOG = {"gl64": 12, "u32": 13}
 
