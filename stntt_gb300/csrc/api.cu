@@ -2006,6 +2006,7 @@ int build_part(stntt_ctx *ctx, stntt_batch *bt, int field, const std::vector<con
         if (pl->passes.size() == 1) {
             PassDesc d = pl->passes[0];
             d.tfast = 1;
+            d.vec = 0;  // packed single-pass items keep the 16-points-per-thread layout (TileArgs::vecl = 0)
             batch_shape(d, field);
             smem = std::max(smem, d.smem_bytes);
             const uint32_t a_idx = (uint32_t)pend.size();
@@ -2039,6 +2040,7 @@ int build_part(stntt_ctx *ctx, stntt_batch *bt, int field, const std::vector<con
                        d1.logL <= 11;
             for (const stntt_job *j : cj)
                 vec = vec && ((uintptr_t)j->data & 15u) == 0;
+            d0.vec = d1.vec = 0;  // TileArgs::vecl: set below only where the checks above hold
             if (vec) {
                 d0.vec = d1.vec = V;
                 const uint32_t lv = V == 2 ? 1 : 2;
