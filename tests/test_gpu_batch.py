@@ -224,3 +224,26 @@ def test_batch_vector_lines_items_and_unaligned_fallback(ctx, field):
             want = O.ntt_u32(x, root, p, inverse=bool(i % 2))
             got = v.cpu().numpy().view(np.uint32)
         assert np.array_equal(got, want), (field, sizes[i])
+
+
+def test_batched_plan_with_vector_flag_keeps_checks(ctx):
+    """A batched-launch plan whose passes carry STNTT_PASS_VEC does not put
+    unaligned jobs on the vector-lines items: the batch's own alignment check
+    decides. Against the oracle."""
+    try:
+        ctx.set_plan(st.FIELD_GL64, 15, [7, 8], elems=[8 | st.PASS_VEC] * 2, cols=[8, 8], batched=True)
+        buf = torch.zeros(2 * (1 << 15) + 4, dtype=torch.int64, device="cuda")
+        xs = [O.uniform_u64(77 + i, 1 << 15) for i in range(2)]
+        views = [buf[1: 1 + (1 << 15)], buf[(1 << 15) + 3: (1 << 15) + 3 + (1 << 15)]]
+        for v, x in zip(views, xs):
+            v.copy_(torch.from_numpy(x.view(np.int64)))
+        assert all(v.data_ptr() % 16 == 8 for v in views)
+        jobs = [st.Job(st.FIELD_GL64, 15, i, 0, 0, 0, v.data_ptr()) for i, v in enumerate(views)]
+        ctx.ntt_batch(jobs)
+        torch.cuda.synchronize()
+        for i, (v, x) in enumerate(zip(views, xs)):
+            assert np.array_equal(v.cpu().numpy().view(np.uint64), O.ntt_gl64(x, inverse=bool(i)))
+    finally:
+        ctx.clear_plans()
+        from stntt_gb300 import tune
+        tune.apply_cache(ctx)
