@@ -131,7 +131,9 @@ cudaError_t launch_tile_vec(int field, const PassDesc &d, uint32_t p, const void
         return d.pow2 == 1   ? launch_tile_vec_gl64f(d, tables, in, out, batch, s)
                : d.pow2 == 2 ? launch_tile_vec_gl64i(d, tables, in, out, batch, s)
                              : cudaErrorNotSupported;
-    if (p < (1u << 30))  // the lazy 32-bit field (every findParams prime up to 2^26)
+    // the lazy 32-bit field with bound-tracked DFTs, which need 8p < 2^32
+    // (every findParams prime up to n = 2^26); other primes take the plain tile
+    if (p < (1u << 29))
         return launch_tile_vec_u32l(d, p, tables, in, out, batch, s);
     return cudaErrorNotSupported;
 }
@@ -1965,10 +1967,13 @@ int build_part(stntt_ctx *ctx, stntt_batch *bt, int field, const std::vector<con
                size_t &scratch_cursor) {
     std::map<ClassKey, std::vector<const stntt_job *>> classes;
     bool lazy = field == kFieldU32;  // the part's kernel: the lazy 32-bit field when every p < 2^30
+    bool lazy8 = lazy;               // and its vector-lines items when every p < 2^29 (8p < 2^32)
     for (const stntt_job *j : jobs) {
         classes[{j->log_n, j->dir, field == kFieldGL ? 0u : j->p, field == kFieldGL ? 0u : j->root}].push_back(j);
         if (field == kFieldU32 && j->p >= (1u << 30))
             lazy = false;
+        if (field == kFieldU32 && j->p >= (1u << 29))
+            lazy8 = false;
     }
     const size_t asz = args_size(field);
     std::vector<unsigned char> args;                   // TileArgs, by value
@@ -2033,9 +2038,9 @@ int build_part(stntt_ctx *ctx, stntt_batch *bt, int field, const std::vector<con
             // and the column pass has a full four-step table (16-byte aligned:
             // an even entry offset from the 256-byte aligned table
             // allocation); for the 32-bit field only in a part of the lazy
-            // field (every p < 2^30), whose kernel has these steps.
+            // field whose primes leave the steps' headroom (every p < 2^29).
             const uint32_t V = field == kFieldGL ? 2 : 4, w = field == kFieldGL ? 8 : 4;
-            bool vec = (field == kFieldGL || lazy) && batch_vec_items() && d0.full_off != ~0ull &&
+            bool vec = (field == kFieldGL || lazy8) && batch_vec_items() && d0.full_off != ~0ull &&
                        (d0.full_off & 1u) == 0 && !d0.full_mont && d0.logL >= 4 && d0.logL <= 11 && d1.logL >= 4 &&
                        d1.logL <= 11;
             for (const stntt_job *j : cj)

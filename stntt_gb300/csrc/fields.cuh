@@ -77,7 +77,30 @@ struct FieldU32L {
         const uint32_t m = lo * pinv;
         return hi + __umulhi(m, p) + (lo != 0u);
     }
+    // Wider headroom for p < 2^29 (8p < 2^32), used by the vector-lines DFT
+    // (dft_lazy): a value below B p with B <= 8 stays a 32-bit number, a
+    // Shoup product of it still lands in [0, 2p), and so does a Montgomery
+    // product (a wr + m p) / 2^32 < (8p^2 + 2^32 p) / 2^32 < 2p.
+    // red(a, K): a in [0, 2K p) -> [0, K p) (one conditional subtraction).
+    __device__ __forceinline__ T red(T a, uint32_t k) const { return min(a, a - k * p); }
+    // a in [0, B p) -> [0, p) by halving steps.
+    template <int B>
+    __device__ __forceinline__ T canon_b(T a) const {
+        if constexpr (B > 4)
+            a = red(a, 4);
+        if constexpr (B > 2)
+            a = red(a, 2);
+        if constexpr (B > 1)
+            a = red(a, 1);
+        return a;
+    }
 };
+
+// Fields whose vector-lines steps track value bounds (FieldU32L with p < 2^29).
+template <class F>
+struct IsLazyBound : std::false_type {};
+template <>
+struct IsLazyBound<FieldU32L> : std::true_type {};
 
 struct FieldGL {
     using T = uint64_t;

@@ -97,8 +97,9 @@ struct VGeo {
 };
 
 // FULL4: 0 two-level four-step lookup, 1 full table of twiddle entries,
-// 2 full table of 4-byte Montgomery entries (32-bit field).
-template <class F, int V, bool COL, int FULL4>
+// 2 full table of 4-byte Montgomery entries (32-bit field). BIN: the values
+// arrive below BIN p (lazy 32-bit field; a four-step product leaves 2p).
+template <class F, int V, bool COL, int FULL4, int BIN = 2>
 __device__ __forceinline__ void vstore_last(const TileArgs<F> &a, const F &f, const VGeo<typename F::T, V> &geo,
                                             uint32_t pos, typename F::T (&v)[V]) {
     using TW = typename F::TW;
@@ -127,8 +128,12 @@ __device__ __forceinline__ void vstore_last(const TileArgs<F> &a, const F &f, co
         }
     }
 #pragma unroll
-    for (int i = 0; i < V; ++i)
-        v[i] = f.canon(v[i]);
+    for (int i = 0; i < V; ++i) {
+        if constexpr (IsLazyBound<F>::value && !COL && BIN > 2)
+            v[i] = f.template canon_b<BIN>(v[i]);
+        else
+            v[i] = f.canon(v[i]);
+    }
     v16_store<typename F::T, V>(geo.dst + (uint64_t)pos * geo.ostride, v);
 }
 
@@ -149,6 +154,105 @@ __device__ __forceinline__ constexpr uint32_t vpoint(uint32_t point) {
     return PB ? point * C + (point >> PB) * V : point * C;
 }
 
+// ---- The R-point DIF network of dft_reg with bounds tracked at compile time
+// (FieldU32L, p < 2^29). Every value is below B p for a known B <= 8, so a sum
+// is one add (a + b < 8p), a difference one add (a - b + K p, K >= the bound
+// of b), and a value is halved (red: one conditional subtraction) only where
+// a butterfly would otherwise pass 8p; twiddled differences leave the Shoup
+// product in [0, 2p). dft_reg keeps every sum and untwiddled difference in
+// [0, 2p) (three operations each). Operation counts per 16-point DFT whose
+// point 0 is below 8p and the others below 2p (later steps): 149 against
+// 209; all inputs canonical (first step): 131. Outputs stay below LzPlan::bout
+// p (8 for R >= 4), canonicalised once before the HBM store.
+template <int R>
+struct LzPlan {
+    int ra[4][8], rb[4][8];  // per level and butterfly: halve a / b first (K, or 0)
+    int kd[4][8];            // K of the difference a - b + K p
+    int bout;                // bound of every output
+};
+
+__host__ __device__ constexpr int lz_pow2_at_least(int b) {
+    int k = 1;
+    while (k < b)
+        k *= 2;
+    return k;
+}
+
+// b0: bound of point 0 (not twiddled by the step), br: of the others.
+template <int R>
+__host__ __device__ constexpr LzPlan<R> lz_plan(int b0, int br) {
+    LzPlan<R> P{};
+    int B[16] = {};
+    for (int i = 0; i < R; ++i)
+        B[i] = i == 0 ? b0 : br;
+    int l = 0;
+    for (int h = R / 2; h >= 1; h /= 2, ++l) {
+        int q = 0;
+        for (int base = 0; base < R; base += 2 * h) {
+            for (int j = 0; j < h; ++j, ++q) {
+                const int a = base + j, b = a + h;
+                // halve the larger input (to below K p, 2K >= its bound) until
+                // the sum and the difference stay below 8p
+                while (B[a] + B[b] > 8 || B[a] + lz_pow2_at_least(B[b]) > 8) {
+                    const int x = B[a] >= B[b] ? a : b;
+                    const int k = lz_pow2_at_least(B[x]) / 2;
+                    int &slot = x == a ? P.ra[l][q] : P.rb[l][q];
+                    if (slot != 0 || k == 0)
+                        return LzPlan<R>{};  // bout 0: no plan (one halving per input)
+                    slot = k;
+                    B[x] = k;
+                }
+                P.kd[l][q] = lz_pow2_at_least(B[b]);
+                const int s = B[a] + B[b];
+                B[b] = j == 0 ? B[a] + P.kd[l][q] : 2;
+                B[a] = s;
+            }
+        }
+    }
+    P.bout = 1;
+    for (int i = 0; i < R; ++i)
+        P.bout = B[i] > P.bout ? B[i] : P.bout;
+    return P;
+}
+
+template <int R>
+__host__ __device__ constexpr int lz_levels() {
+    return R == 2 ? 1 : R == 4 ? 2 : R == 8 ? 3 : 4;
+}
+
+// Level L, butterfly Q of the network (same order and twiddles as dft_reg).
+template <class F, int R, int B0, int BR, int L = 0, int Q = 0>
+__device__ __forceinline__ void dft_lazy(const F &f, typename F::T *x, const typename F::TW *w16) {
+    static_assert(IsLazyBound<F>::value, "bound-tracked DFT of the lazy 32-bit field");
+    if constexpr (L < lz_levels<R>()) {
+        constexpr LzPlan<R> P = lz_plan<R>(B0, BR);
+        static_assert(P.bout >= 1 && P.bout <= 8, "values stay below 8p");
+        constexpr int h = (R / 2) >> L, j = Q % h, a = (Q / h) * 2 * h + j, b = a + h;
+        if constexpr (P.ra[L][Q] != 0)
+            x[a] = f.red(x[a], P.ra[L][Q]);
+        if constexpr (P.rb[L][Q] != 0)
+            x[b] = f.red(x[b], P.rb[L][Q]);
+        const uint32_t d = x[a] - x[b] + (uint32_t)P.kd[L][Q] * f.p;
+        x[a] = x[a] + x[b];
+        if constexpr (j == 0)
+            x[b] = d;
+        else
+            x[b] = f.mul_tw(d, w16[j * (16 / (2 * h))]);
+        if constexpr (Q + 1 < R / 2)
+            dft_lazy<F, R, B0, BR, L, Q + 1>(f, x, w16);
+        else
+            dft_lazy<F, R, B0, BR, L + 1, 0>(f, x, w16);
+    }
+}
+
+// Bounds entering a vector-lines step's DFTs: the first reads canonical
+// values from HBM; later ones read point 0 as the previous step left it
+// (below 8p) and the others after a Shoup product (below 2p).
+template <bool first>
+struct LzIn {
+    static constexpr int b0 = first ? 1 : 8, br = first ? 1 : 2;
+};
+
 // One radix-2^LOGR Stockham step over the tile (see tile_step_l): read R
 // points per item (HBM on the first step, else shared memory), twiddle,
 // R-point DFT per line, write R points (shared memory, or HBM on the last).
@@ -160,6 +264,8 @@ __device__ __forceinline__ void vstep(const TileArgs<F> &a, const F &f, typename
     constexpr uint32_t U = (1u << LOGL) / E, TS = (1u << LOGL) >> LOGR, P = 1u << LOGP, C = V << LOGG;
     static_assert(LOGR + LOGP <= LOGL, "step beyond the tile");
     const auto at = [](uint32_t point) { return vpoint<V, LOGG>(point); };
+    // bound of this step's outputs (lazy 32-bit field), else canonical-ish 2
+    constexpr int kBout = IsLazyBound<F>::value ? lz_plan<R>(LzIn<first>::b0, LzIn<first>::br).bout : 2;
     if constexpr (last)
         pdl_trigger();
     // ---- read R points per item: idx = u + m U + r L/R
@@ -199,8 +305,12 @@ __device__ __forceinline__ void vstep(const TileArgs<F> &a, const F &f, typename
             }
         }
 #pragma unroll
-        for (int i = 0; i < V; ++i)
-            dft_reg<F, R>(f, &x[i][m * R], a.wR);
+        for (int i = 0; i < V; ++i) {
+            if constexpr (IsLazyBound<F>::value)
+                dft_lazy<F, R, LzIn<first>::b0, LzIn<first>::br>(f, &x[i][m * R], a.wR);
+            else
+                dft_reg<F, R>(f, &x[i][m * R], a.wR);
+        }
     }
     if constexpr (!first && !last)
         __syncthreads();  // every read of this step precedes any write
@@ -218,7 +328,7 @@ __device__ __forceinline__ void vstep(const TileArgs<F> &a, const F &f, typename
             for (int i = 0; i < V; ++i)
                 v[i] = x[i][m * R + bit_reverse<LOGR>(r)];
             if constexpr (last)
-                vstore_last<F, V, COL, FULL4>(a, f, geo, pos, v);
+                vstore_last<F, V, COL, FULL4, kBout>(a, f, geo, pos, v);
             else
                 v16_store<T, V>(sm_g + at(pos), v);
         }

@@ -226,6 +226,32 @@ def test_batch_vector_lines_items_and_unaligned_fallback(ctx, field):
         assert np.array_equal(got, want), (field, sizes[i])
 
 
+def test_batch_u32_prime_above_2e29_keeps_plain_items(ctx):
+    """A 32-bit batch with one job over a prime in [2^29, 2^30) runs its
+    two-pass classes on the 16-points-per-thread items (the vector-lines
+    items need 8p < 2^32); every job, the per-size primes' too, against the
+    oracle."""
+    sizes = [14, 15, 17, 15]
+    jobs, bufs, inputs, params = [], [], [], []
+    for i, s in enumerate(sizes):
+        if i == 3:
+            root, p = st.findParams(1 << s, 1 << 29)
+            assert (1 << 29) <= p < (1 << 30)
+        else:
+            p, root = st.params_u32(s)
+        x = O.uniform_u32(515 + i, p, 1 << s)
+        d = torch.from_numpy(x.view(np.int32).copy()).cuda()
+        jobs.append(st.Job(st.FIELD_U32, s, i % 2, p, root, 0, d.data_ptr()))
+        bufs.append(d)
+        inputs.append(x)
+        params.append((p, root))
+    ctx.ntt_batch(jobs)
+    torch.cuda.synchronize()
+    for i, (d, x, (p, root)) in enumerate(zip(bufs, inputs, params)):
+        want = O.ntt_u32(x, root, p, inverse=bool(i % 2))
+        assert np.array_equal(d.cpu().numpy().view(np.uint32), want), (i, sizes[i])
+
+
 def test_batched_plan_with_vector_flag_keeps_checks(ctx):
     """A batched-launch plan whose passes carry STNTT_PASS_VEC does not put
     unaligned jobs on the vector-lines items: the batch's own alignment check

@@ -373,6 +373,23 @@ def test_u32_primes_above_2e30(ctx, lg):
 
 
 
+@pytest.mark.parametrize("lg", [10, 14, 20, 22])
+def test_u32_primes_between_2e29_and_2e30(ctx, lg):
+    """Primes in [2^29, 2^30) keep the lazy field but not the vector-lines
+    steps, whose bound-tracked DFTs need 8p < 2^32: their plans fall back to
+    the plain tile. Single and batched transforms against the oracle, and the
+    round trip."""
+    root, p = st.findParams(1 << lg, 1 << 29)
+    assert (1 << 29) <= p < (1 << 30)
+    for batch in (1, 2):
+        x = O.uniform_u32(31 + lg + batch, p, batch << lg)
+        d = dev32(x)
+        ctx.ntt_u32(d, lg, batch, p, root)
+        assert np.array_equal(host32(d), O.ntt_u32(x, root, p, batch=batch)), (lg, batch)
+        ctx.ntt_u32(d, lg, batch, p, root, inverse=True)
+        assert np.array_equal(host32(d), x), (lg, batch)
+
+
 def _gl_add(a, b):
     """(a + b) mod p for canonical uint64 arrays, with wrap-around arithmetic."""
     with np.errstate(over="ignore"):
