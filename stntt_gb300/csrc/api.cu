@@ -537,6 +537,20 @@ uint32_t full_twiddle_max_log_small(bool vec) {
     return vec ? v : plain;
 }
 
+// Smallest column-pass sub-problem (log2 points) whose full four-step table
+// holds 4-byte Montgomery entries in the 32-bit vector-lines build, for calls
+// of 2^22+ elements: 2^17 (kFullMontMinLog), or STNTT_FULL_MONT_MIN_LOG
+// (14..26) from the environment, read once. Half the bytes of a Shoup pair
+// per element for one more multiply: the 2^17-point table of the second pass
+// of a 2^26-point transform stays in L2 either way, but its 8-byte loads kept
+// the L1 data pipe busy (measured forward + inverse 0.808 -> 0.800 ms).
+// Small calls and batched plans keep Shoup pairs up to 2^20 points (the
+// batched items read Shoup tables only).
+uint32_t full_mont_min_log(bool small_or_batched) {
+    static const uint32_t v = env_log_limit("STNTT_FULL_MONT_MIN_LOG", kFullMontMinLog);
+    return small_or_batched ? kFullTwiddleMaxLog + 1 : v;
+}
+
 // -p^-1 mod 2^32 for odd p (Newton's iteration doubles the correct low bits).
 uint32_t neg_inv32(uint32_t p) {
     uint32_t x = p;  // p * p = 1 mod 8: three bits
@@ -547,7 +561,7 @@ uint32_t neg_inv32(uint32_t p) {
 
 // Build the pass list and the twiddle tables for one transform.
 int build_plan(stntt_ctx *ctx, Plan &pl, int field, uint32_t log_n, uint32_t p, uint64_t root_dir, int dir,
-               const PlanSpec *spec, bool small_call) {
+               const PlanSpec *spec, bool small_call, bool batched) {
     pl.field = field;
     pl.log_n = log_n;
     pl.p = p;
@@ -662,7 +676,10 @@ int build_plan(stntt_ctx *ctx, Plan &pl, int field, uint32_t log_n, uint32_t p, 
             // entries are 4-byte Montgomery values instead of 8-byte Shoup
             // pairs (a 2^26-point table: 256 MiB instead of 512 MiB to read
             // beside the 256 MiB of data), at two more multiplies per product.
-            d.full_mont = (field != kFieldGL && d.vec && d.logM > kFullTwiddleMaxLog && p < (1u << 30)) ? 1 : 0;
+            d.full_mont =
+                (field != kFieldGL && d.vec && d.logM >= full_mont_min_log(small_call || batched) && p < (1u << 29))
+                    ? 1
+                    : 0;
             d.pinv = d.full_mont ? neg_inv32(p) : 0;
             d.full_off = add_full(1ull << d.logM, d.lo_off, d.hi_off, d.h, d.logS, d.full_mont != 0);
         }
@@ -715,7 +732,8 @@ int get_plan(stntt_ctx *ctx, int field, uint32_t log_n, uint32_t p, uint64_t roo
     if (has_spec)
         spec = sit->second;
     ctx->mu.unlock();
-    int rc = build_plan(ctx, *pl, field, log_n, p, rd, dir, has_spec ? &spec : nullptr, small_call);
+    int rc = build_plan(ctx, *pl, field, log_n, p, rd, dir, has_spec ? &spec : nullptr, small_call,
+                        kind == kPlanBatched);
     ctx->mu.lock();
     if (rc != STNTT_OK) {
         if (pl->d_tables)

@@ -26,6 +26,9 @@ constexpr uint32_t kFullTwiddleMaxLogSmallVec = 21;
 // Passes in the vector-lines build (tile_v.cuh) of calls of 2^22+ elements
 // use full tables up to 2^26-point sub-problems (see build_plan).
 constexpr uint32_t kFullTwiddleMaxLogVec = 26;
+// 32-bit vector-lines column passes of calls of 2^22+ elements: Montgomery
+// table entries from 2^17-point sub-problems on (api.cu, full_mont_min_log)
+constexpr uint32_t kFullMontMinLog = 17;
 // One-launch transforms: 16-CTA clusters (non-portable size) where the device
 // schedules them, else 8; up to 2^(15 + log2 K) bytes per transform.
 constexpr uint32_t kClusterLogSmall = 3, kClusterLogLarge = 4;
