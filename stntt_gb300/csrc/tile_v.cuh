@@ -163,7 +163,7 @@ __device__ __forceinline__ constexpr uint32_t vpoint(uint32_t point) {
 // [0, 2p) (three operations each). Operation counts per 16-point DFT whose
 // point 0 is below 8p and the others below 2p (later steps): 149 against
 // 209; all inputs canonical (first step): 131. Outputs stay below LzPlan::bout
-// p (8 for R >= 4), canonicalised once before the HBM store.
+// p (at most 8), canonicalised once before the HBM store.
 template <int R>
 struct LzPlan {
     int ra[4][8], rb[4][8];  // per level and butterfly: halve a / b first (K, or 0)
