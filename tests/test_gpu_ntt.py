@@ -708,6 +708,7 @@ def test_vector_lines_build(ctx, field, lg, logs, batch, cols):
     fid = st.FIELD_GL64 if field == "gl64" else st.FIELD_U32
     k = len(logs)
     try:
+        ctx.clear_plans()  # without the packaged small-call shapes, calls under 2^22 elements take this plan too
         ctx.set_plan(fid, lg, logs, elems=[16 | VEC] * k, cols=[cols] * k)
         n = 1 << lg
         if field == "gl64":
@@ -856,6 +857,7 @@ def test_gl64_edge_values(ctx, lg, logs, elems, cols):
     try:
         for plan in ("tuned", "vec"):
             if plan == "vec":
+                ctx.clear_plans()  # the packaged small-call shape would take a single 2^16 / 2^20 call
                 ctx.set_plan(st.FIELD_GL64, lg, logs, elems=[elems | VEC] * len(logs), cols=[cols] * len(logs))
             for inv in (False, True):
                 d = dev64(x)
@@ -883,6 +885,7 @@ def test_vector_lines_cluster_pass(ctx, field, lg, logs, cols, batch):
     fid = st.FIELD_GL64 if field == "gl64" else st.FIELD_U32
     elems = [(8 | VEC | CL) if lg_ >= 11 else (8 | VEC) for lg_ in logs]
     try:
+        ctx.clear_plans()  # without the packaged small-call shapes, calls under 2^22 elements take this plan too
         ctx.set_plan(fid, lg, logs, elems=elems, cols=[cols] * len(logs))
         n = 1 << lg
         for inv in (False, True):
@@ -946,6 +949,7 @@ def test_vector_lines_four_points_per_line(ctx, field, lg, logs, cols):
     single small transforms, forward and inverse against the oracle."""
     fid = st.FIELD_GL64 if field == "gl64" else st.FIELD_U32
     try:
+        ctx.clear_plans()  # without the packaged small-call shapes, single calls take this plan
         ctx.set_plan(fid, lg, logs, elems=[4 | VEC] * len(logs), cols=cols)
         n = 1 << lg
         for inv in (False, True):

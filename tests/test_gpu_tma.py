@@ -75,6 +75,7 @@ GL_CASES = [
 @pytest.mark.parametrize("lg,batch,logs,cols", GL_CASES)
 def test_gl64_staged_equals_oracle(tctx, lg, batch, logs, cols):
     if logs:
+        tctx.clear_plans()  # without the packaged small-call shapes, calls under 2^22 elements take this plan too
         tctx.set_plan(GL, lg, logs, cols=cols)
     try:
         x = O.uniform_u64(700 + lg, batch << lg)
@@ -102,8 +103,9 @@ U32_CASES = [
 def test_u32_staged_equals_plain(tctx, ctx, lg, batch, logs, cols):
     p, root = st.params_u32(lg)
     if logs:
-        tctx.set_plan(U32, lg, logs, cols=cols)
-        ctx.set_plan(U32, lg, logs, cols=cols)
+        for c in (tctx, ctx):
+            c.clear_plans()  # without the packaged small-call shapes, calls under 2^22 elements take this plan too
+            c.set_plan(U32, lg, logs, cols=cols)
     try:
         x = O.uniform_u32(800 + lg, p, batch << lg)
         f = run_u32(tctx, x, lg, batch, p, root)
