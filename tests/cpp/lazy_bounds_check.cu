@@ -5,7 +5,8 @@
 // at the top of their [0, 2p) range, and checks that (a) every halving input
 // lies below 2K p, (b) every sum and difference stays below 8p (so the
 // 32-bit kernel never wraps), (c) every output lies below the plan's bout,
-// and (d) the outputs are congruent to the exact DIF network mod p.
+// and (d) the outputs are congruent to the exact DIF network mod p; and
+// that the Shoup and Montgomery products keep inputs below 8p in [0, 2p).
 // Prints the violations it finds and a summary line; exits non-zero on any.
 #include <cstdint>
 #include <cstdio>
@@ -124,6 +125,33 @@ static int canon_check(uint64_t p) {
     return bad;
 }
 
+// The two products the steps apply to values below 8p, restated from
+// FieldU32L (fields.cuh): Shoup's a*w - floor(a*w'/2^32)*p for any 32-bit a,
+// and Montgomery's REDC(a * (w 2^32 mod p)) for a < 8p. Both must land in
+// [0, 2p) and be congruent to a*w.
+static int product_check(uint64_t p, std::mt19937_64 &rng) {
+    int bad = 0;
+    uint32_t pinv = (uint32_t)p;  // -p^-1 mod 2^32 by Newton's iteration
+    for (int i = 0; i < 4; ++i)
+        pinv *= 2u - (uint32_t)p * pinv;
+    pinv = 0u - pinv;
+    for (int t = 0; t < 20000; ++t) {
+        const uint64_t w = rng() % p;
+        const uint32_t wsh = (uint32_t)((w << 32) / p);
+        const uint32_t a32 = t % 3 == 0 ? 0xffffffffu - (uint32_t)(rng() % 4) : (uint32_t)rng();
+        const uint32_t q = (uint32_t)(((uint64_t)a32 * wsh) >> 32);
+        const uint32_t r = a32 * (uint32_t)w - q * (uint32_t)p;
+        bad += r >= 2 * p || r % p != (uint64_t)a32 * w % p;
+        const uint64_t a = t % 3 == 0 ? 8 * p - 1 - rng() % 4 : rng() % (8 * p);
+        const uint32_t wr = (uint32_t)((w << 32) % p);
+        const uint32_t lo = (uint32_t)a * wr, hi = (uint32_t)((a * wr) >> 32);
+        const uint32_t m = lo * pinv;
+        const uint64_t red = (uint64_t)hi + (((uint64_t)m * p) >> 32) + (lo != 0u);
+        bad += red >= 2 * p || red % p != a * w % p;
+    }
+    return bad;
+}
+
 int main() {
     std::mt19937_64 rng(12345);
     // every findParams prime up to n = 2^26 and the largest prime below 2^29
@@ -132,6 +160,7 @@ int main() {
     int bad = 0;
     for (uint64_t p : primes) {
         bad += canon_check(p);
+        bad += product_check(p, rng);
         for (int first = 0; first < 2; ++first) {
             const int b0 = first ? LzIn<true>::b0 : LzIn<false>::b0, br = first ? LzIn<true>::br : LzIn<false>::br;
             bad += run<2>(p, b0, br, rng, 2000);
