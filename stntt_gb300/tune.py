@@ -146,27 +146,43 @@ def candidates(field: int, log_n: int, full: bool = False,
 
 
 def _time_plan(ctx: st.Context, field: int, log_n: int, data, p: int, root: int, batch: int, reps: int,
-               flush) -> float:
+               flush, inverse_too: bool = False) -> float:
     """Mean device time of one forward call (CUDA events around each call),
     with L2 flushed before every call as in bench.py. Calls of fewer than 2^22
     elements are captured once as a CUDA graph and replayed, as bench.py times
-    them (a direct call's host work can leave gaps between its kernels)."""
+    them (a direct call's host work can leave gaps between its kernels).
+    inverse_too: time bench.py's step instead, the forward call then the
+    inverse (one graph each)."""
     import torch
 
     stream = torch.cuda.Stream(device=data.device)
     sp = stream.cuda_stream
-    run = (lambda: ctx.ntt_gl64(data, log_n, batch, stream=sp)) if field == st.FIELD_GL64 else \
-        (lambda: ctx.ntt_u32(data, log_n, batch, p, root, stream=sp))
+
+    def call(inv: bool):
+        if field == st.FIELD_GL64:
+            return lambda: ctx.ntt_gl64(data, log_n, batch, inverse=inv, stream=sp)
+        return lambda: ctx.ntt_u32(data, log_n, batch, p, root, inverse=inv, stream=sp)
+
+    runs = [call(False), call(True)] if inverse_too else [call(False)]
     with torch.cuda.stream(stream):
-        run()
+        for run in runs:
+            run()
         stream.synchronize()
         if (batch << log_n) < (1 << 22):
-            graph = torch.cuda.CUDAGraph()
-            with torch.cuda.graph(graph, stream=stream, capture_error_mode="relaxed"):
-                run()
-            step = graph.replay
+            graphs = []
+            for run in runs:
+                graph = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(graph, stream=stream, capture_error_mode="relaxed"):
+                    run()
+                graphs.append(graph)
+            parts = [g.replay for g in graphs]
         else:
-            step = run
+            parts = runs
+
+        def step():
+            for part in parts:
+                part()
+
         step()
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
         for a, b in ev:
@@ -179,9 +195,11 @@ def _time_plan(ctx: st.Context, field: int, log_n: int, data, p: int, root: int,
 
 
 def tune(ctx: st.Context, field: int, log_n: int, reps: int = 10, full: bool = False, verbose: bool = False,
-         batch: int = 0, vec: bool = False):
+         batch: int = 0, vec: bool = False, verify: int = 0):
     """Return (best_spec, best_us, all_results) for one size; leaves the best plan set.
-    batch 0: enough transforms for 2^24 elements (a GPU-filling batch)."""
+    batch 0: enough transforms for 2^24 elements (a GPU-filling batch).
+    verify k > 1: re-time the k fastest forward candidates as forward + inverse
+    steps and keep the fastest of those (verify_top)."""
     import torch
 
     batch = batch or max(1, (1 << 24) >> log_n)
@@ -210,8 +228,29 @@ def tune(ctx: st.Context, field: int, log_n: int, reps: int = 10, full: bool = F
             print(f"{logs} E={es} C={cs}: {us:.1f} us", flush=True)
     results.sort(key=lambda r: r["us"])
     best = results[0]
+    if verify > 1:
+        def step_us(r):
+            ctx.set_plan(field, log_n, r["logs"], r["E"], r["C"], small=small)
+            return _time_plan(ctx, field, log_n, data, p, root, batch, reps, flush, inverse_too=True)
+
+        best = verify_top(results, verify, step_us)[0]
+        if verbose:
+            print(f"verified {verify}: {best['logs']} E={best['E']} C={best['C']}: {best['step_us']:.1f} us per "
+                  "forward + inverse", flush=True)
     ctx.set_plan(field, log_n, best["logs"], best["E"], best["C"], small=small)
     return best, results
+
+
+def verify_top(results: list[dict], k: int, step_us) -> list[dict]:
+    """The k fastest forward-only candidates (results sorted by "us"), each
+    given "step_us" = step_us(candidate) (bench.py's forward + inverse step),
+    sorted by it. The forward-only ranking can miss: at Goldilocks 2^20 it put
+    [10, 10] (4 and 16 points per line) level with [11, 9], which the bench's
+    step times at 67.5 against 60.9 us."""
+    top = results[:k]
+    for r in top:
+        r["step_us"] = step_us(r)
+    return sorted(top, key=lambda r: r["step_us"])
 
 
 def batched_candidates(log_n: int) -> list[list[int]]:
@@ -366,6 +405,8 @@ def main() -> None:
     ap.add_argument("--batched", action="store_true",
                     help="tune the pass split of jobs in the persistent batched launch instead")
     ap.add_argument("--vec", action="store_true", help="also try the vector-lines build of three-pass splits")
+    ap.add_argument("--verify", type=int, default=0,
+                    help="re-time the k fastest forward candidates as forward + inverse steps (bench.py's step)")
     args = ap.parse_args()
     field = st.FIELD_GL64 if args.field == "gl64" else st.FIELD_U32
     ctx = st.Context(0)
@@ -377,7 +418,7 @@ def main() -> None:
             allres[f"{args.field}:{lg}:batch"] = res
             print(json.dumps({"size": f"{args.field}:{lg}:batch", "best": best, "candidates": len(res)}), flush=True)
             continue
-        best, res = tune(ctx, field, lg, args.reps, args.full, args.verbose, args.batch, args.vec)
+        best, res = tune(ctx, field, lg, args.reps, args.full, args.verbose, args.batch, args.vec, args.verify)
         record(ctx, field, lg, best, Path(args.cache))
         allres[f"{args.field}:{lg}" + (":b1" if (best["batch"] << lg) < (1 << 22) else "")] = res
         print(json.dumps({"size": f"{args.field}:{lg}", "best": best, "candidates": len(res)}), flush=True)

@@ -126,3 +126,99 @@ def test_plan_candidates_offer_cluster_passes():
     mixed = [c for c in tune.candidates(st.FIELD_GL64, 20, vec=True) if any(e & cl for e in c[1])]
     assert ([11, 9], [8 | st.PASS_VEC | cl, 8 | st.PASS_VEC], [8, 8]) in mixed
     assert all(len(logs) == 2 for logs, _, _ in u + g + mixed)
+
+
+def test_verify_top_reranks_by_step_time():
+    """--verify: the k fastest forward-only candidates are re-timed as forward
+    + inverse steps and ranked by that time; the others are not timed again."""
+    results = [{"logs": [10, 10], "us": 29.5}, {"logs": [11, 9], "us": 29.6}, {"logs": [9, 11], "us": 30.5},
+               {"logs": [12, 8], "us": 40.0}]
+    step = {(10, 10): 67.5, (11, 9): 60.9, (9, 11): 62.0}
+    timed = []
+
+    def step_us(r):
+        timed.append(tuple(r["logs"]))
+        return step[tuple(r["logs"])]
+
+    ranked = tune.verify_top(results, 3, step_us)
+    assert [r["logs"] for r in ranked] == [[11, 9], [9, 11], [10, 10]]
+    assert ranked[0]["step_us"] == 60.9
+    assert sorted(timed) == sorted(step) and "step_us" not in results[3]
+
+
+def test_time_plan_step_orchestration(monkeypatch):
+    """_time_plan's call sequence, with torch.cuda faked on the CPU: a small
+    call is captured as one graph per direction and each timed step replays
+    the forward graph then (inverse_too) the inverse one; a large call runs
+    the C-ABI calls directly."""
+    import contextlib
+
+    import torch
+
+    log = []
+
+    class _Stream:
+        cuda_stream = 1234
+
+        def __init__(self, device=None):
+            pass
+
+        def synchronize(self):
+            log.append("sync")
+
+    class _Graph:
+        n = 0
+
+        def __init__(self):
+            _Graph.n += 1
+            self.id = _Graph.n
+
+        def replay(self):
+            log.append(f"replay{self.id}")
+
+    capturing = []
+
+    @contextlib.contextmanager
+    def _graph(g, stream=None, capture_error_mode=None):
+        capturing.append(g.id)
+        yield
+        capturing.pop()
+
+    class _Event:
+        def __init__(self, enable_timing=False):
+            pass
+
+        def record(self, stream=None):
+            log.append("event")
+
+        def elapsed_time(self, other):
+            return 0.01
+
+    monkeypatch.setattr(torch.cuda, "Stream", _Stream)
+    monkeypatch.setattr(torch.cuda, "stream", lambda s: contextlib.nullcontext())
+    monkeypatch.setattr(torch.cuda, "CUDAGraph", _Graph)
+    monkeypatch.setattr(torch.cuda, "graph", _graph)
+    monkeypatch.setattr(torch.cuda, "Event", _Event)
+    monkeypatch.setattr(torch.cuda, "synchronize", lambda *a: None)
+
+    class _Ctx:
+        def ntt_gl64(self, data, log_n, batch, inverse=False, stream=None):
+            assert stream == 1234
+            log.append(("inv" if inverse else "fwd") + (f"@g{capturing[-1]}" if capturing else ""))
+
+    class _Data:
+        device = "cpu"
+
+    class _Flush:
+        def zero_(self):
+            log.append("flush")
+
+    us = tune._time_plan(_Ctx(), st.FIELD_GL64, 20, _Data(), 0, 0, 1, 2, _Flush(), inverse_too=True)
+    assert abs(us - 10.0) < 1e-9
+    g1, g2 = _Graph.n - 1, _Graph.n
+    assert log[:5] == ["fwd", "inv", "sync", f"fwd@g{g1}", f"inv@g{g2}"]
+    timed = log[7:]  # after the warm-up replay of both graphs
+    assert timed == ["flush", "event", f"replay{g1}", f"replay{g2}", "event"] * 2
+    log.clear()
+    tune._time_plan(_Ctx(), st.FIELD_GL64, 22, _Data(), 0, 0, 1, 1, _Flush())
+    assert log == ["fwd", "sync", "fwd", "flush", "event", "fwd", "event"]
